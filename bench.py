@@ -1,0 +1,338 @@
+"""Benchmark of the MRG8 bulk path on GB300 (one JSON line on rank 0).
+
+Workload (one step): the plain single-stream generator writes 2^30 fp64
+uniforms (SHIFTED scaling, [0,1), as cuda/mrg8_cuda.cu's mrg8_outer_32) from
+seed 13579 into an HBM-resident buffer: one launch of the bulk kernel.  The
+output (8 GiB) is larger than L2, so no flush is needed between steps.
+
+  value    whole-job Gsamples/s, device buffer, CUDA events on the launch stream
+  e2e      the same through the C ABI with a pinned HOST buffer
+           (mrg8g_generate_host: device staging + D2H inside the timed region)
+  roofline HBM-write roofline of the bulk kernel against MEASURED_PEAKS.json
+  cpu_baseline  the oracle port of the reference's CPU path on all host cores
+
+``--impl reference`` times the reference's CPU implementation of the path
+(the build in oracle/_ref where it exists, else the oracle port) on the same
+metric.  Under torchrun each rank generates its own 2^30-output shard of one
+stream (rank r starts r * 2^30 outputs in; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 13579
+N_PER_RANK = 1 << 30
+METRIC = "fp64 Gsamples/s & %HBM peak at 2^30; batched vs per-call speedup; served p50/p99"
+UNIT = "Gsamples/s"
+WORKLOAD = "plain MRG8 single stream: 2^30 fp64 uniforms (SHIFTED, [0,1)) from seed 13579 per GPU"
+CPU_SAMPLE_N = 1 << 28
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profiled_traffic(name: str):
+    """Per-launch DRAM bytes recorded from an ncu capture in profiles/<name>."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        text = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", text)
+    return float(m.group(1)) if m else None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        loaded = [v for v in sm if smax and v > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(n: int, kind: int, min_seconds: float = 3.0):
+    """The reference's CPU path on all host cores: the knl/ block-split
+    generator (knl/mrg8_vec.h:500-525, its non-AVX A^8 recurrence), restated
+    in oracle/mrg8_oracle.c.  Returns (Gsamples/s, cores, sample text)."""
+    import numpy as np
+
+    from oracle.pyoracle import KIND_DTYPE, Oracle
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    st = o.seed(SEED)
+    out = np.empty(n, dtype=KIND_DTYPE[kind])
+    o.generate(st, n, kind, nthreads=cores, out=out)  # first run discarded (page faults)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        o.generate(st, n, kind, nthreads=cores, out=out)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds and runs >= 3:
+            break
+    gs = n * runs / el / 1e9
+    return gs, cores, f"{runs} runs of {n} fp64 SHIFTED samples ({n * 8 >> 20} MiB), first run discarded"
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle.pyoracle import F64_SHIFTED, REF_DIR, KIND_DTYPE, Oracle
+    cores = os.cpu_count() or 1
+    kind_name, impl = "port", None
+    refdir = os.environ.get("MRG8_REFERENCE", "/root/reference")
+    if os.path.exists(os.path.join(REF_DIR, "libmrg8_ref_knl.so")) and os.path.isdir(refdir):
+        try:
+            from oracle.pyoracle import RefLib
+            impl = RefLib("knl", refdir)
+            kind_name = "reference"
+        except OSError:
+            impl = None
+    o = Oracle()
+    st = o.seed(SEED)
+    n = CPU_SAMPLE_N
+    out = np.empty(n, dtype=KIND_DTYPE[F64_SHIFTED])
+
+    def step():
+        if impl is not None:
+            impl.rand_tp(st, n, cores)
+        else:
+            o.generate(st, n, F64_SHIFTED, nthreads=cores, out=out)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    value = n * args.steps / el / 1e9
+    sample = (f"each step {n} fp64 SHIFTED samples of the same stream (seed {SEED}), "
+              + ("knl/mrg8.h rand_tp compiled from the reference" if impl is not None else
+                 "oracle port of knl/mrg8_vec.h mrg8_vec_outer_tp (block split + A^8 recurrence)")
+              + f", {cores} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "n": N_PER_RANK, "seed": SEED},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": kind_name,
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import numpy as np
+    import torch
+
+    import mrg8_gb300 as m
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    n = N_PER_RANK
+    kind = m.F64_SHIFTED
+    g = m.MRG8(SEED)
+    if rank:
+        g.jump_ahead(rank * n)           # this rank's shard of the one stream
+    st0 = g.get_state()
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        g.set_state(st0)
+        g.rand(out, scaling=1)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if pg:
+        pg.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if pg:
+        pg.barrier()
+    per = [a.elapsed_time(b) for a, b in evs]          # ms, one launch per step
+    total_ms = sum(per)
+    if pg:
+        t = torch.tensor([total_ms, wall * 1e3], device=dev, dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t[0])
+    value = ws * n * args.steps / (total_ms / 1e3) / 1e9
+    peaks, peak_src = measured_peaks()
+    avg_launch_s = statistics.mean(per) / 1e3
+    achieved = 8.0 * n / avg_launch_s / 1e9
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+
+    # fp32 at the same size (secondary line item; not the headline).
+    out32 = torch.empty(n, dtype=torch.float32, device=dev)
+    for _ in range(3):
+        g.set_state(st0)
+        g.rand_f32(out32, scaling=1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, args.steps // 2)
+    e0.record(stream)
+    for _ in range(reps):
+        g.set_state(st0)
+        g.rand_f32(out32, scaling=1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    f32_s = e0.elapsed_time(e1) / 1e3 / reps
+    del out32
+
+    # End to end through the C ABI with a pinned host buffer.
+    e2e = None
+    if not args.skip_e2e:
+        host = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        hp = host.numpy()
+        for _ in range(2):
+            g.set_state(st0)
+            g._generate(hp, n, kind)
+        if pg:
+            pg.barrier()
+        esteps = max(3, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(esteps):
+            g.set_state(st0)
+            g._generate(hp, n, kind)
+        el = time.perf_counter() - t0
+        if pg:
+            t = torch.tensor([el], device=dev, dtype=torch.float64)
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            el = float(t[0])
+        e2e = {"value": round(ws * n * esteps / el / 1e9, 4), "unit": UNIT, "h2d_bytes_per_step": 32,
+               "d2h_bytes_per_step": 8 * n, "steps": esteps,
+               "path": "mrg8g_generate_host (C ABI) into pinned host memory; the 32-byte state travels as a "
+                       "kernel argument"}
+        del host
+
+    # Spot check of this run's output against the oracle (first 2^20 values).
+    from oracle.pyoracle import F64_SHIFTED as O_F64S, Oracle
+    ref, _ = Oracle().generate(st0, 1 << 20, O_F64S, nthreads=os.cpu_count() or 8)
+    ok = bool(np.array_equal(out[: 1 << 20].cpu().numpy().view(np.uint64), ref.view(np.uint64)))
+
+    if rank != 0:
+        if pg:
+            pg.destroy_process_group()
+        return
+    cpu = None
+    if not args.skip_cpu:
+        v, cores, sample = cpu_baseline(CPU_SAMPLE_N, O_F64S)
+        cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    traffic = profiled_traffic("k_plain_f64_2p30.md")
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "seed": SEED, "layout": "1 warp tile per resident warp, V=2",
+                   "l2": "each step writes 8 GiB (> 129 MB L2): no flush needed", "parallelism": f"shard{ws}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "peak_source": f"{peak_src} hbm_gbs (copy)",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": 8 * n},
+        "f32": {"value": round(n / f32_s / 1e9, 4), "unit": UNIT, "gbs": round(4.0 * n / f32_s / 1e9, 1),
+                "frac_hbm": round(4.0 * n / f32_s / 1e9 / hbm, 4)},
+        "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": args.steps,
+        "parity_spot_check": ok, "wall_s": round(wall, 4),
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,165 @@
+/*
+ * mrg8g.h -- C ABI of the GB300-native MRG8 generator (libmrg8g.so).
+ *
+ * MRG8 is L'Ecuyer's order-8 multiple recursive generator modulo 2^31-1:
+ *     S[n] = sum_{k=1..8} a_k S[n-k]  mod (2^31 - 1),
+ * with the state (S[n-1], ..., S[n-8]) kept newest first.  Every stream
+ * output is the representative in [1, 2^31-1] (0 is represented by 2^31-1),
+ * and every output of this library is bit-identical to the reference's
+ * sequential stream (kenmiura/mrg8 original/mrg8.cpp) for the same state.
+ *
+ * The reference interface is the C++ class pair mrg8 / mrg8_cuda
+ * (original/mrg8.h:21-56, cuda/mrg8.h:23-79, cuda/mrg8_cuda.h:20-45).  Each
+ * entry point below names the member it replaces.  include/mrg8_cuda.hpp
+ * re-creates those classes on top of this ABI.
+ *
+ * Conventions
+ *  - Every function returns MRG8G_SUCCESS (0) or a negative error code;
+ *    mrg8g_last_error() describes the last failure of the calling thread.
+ *  - Device pointers are plain CUDA device addresses on the current device;
+ *    `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Generation calls are stream-ordered and asynchronous; the handle's state
+ *    advances on the host immediately, so the next call may be issued at once.
+ *  - A handle is not thread-safe (neither is the reference); distinct handles
+ *    may be used from distinct threads.
+ *  - Output buffers must be aligned to their element size.
+ */
+#ifndef MRG8G_H
+#define MRG8G_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MRG8G_VERSION 1
+
+#if defined(__GNUC__)
+#define MRG8G_API __attribute__((visibility("default")))
+#else
+#define MRG8G_API
+#endif
+
+/* Return codes. */
+#define MRG8G_SUCCESS 0
+#define MRG8G_ERR_INVALID_ARGUMENT (-1)
+#define MRG8G_ERR_INVALID_STATE (-2) /* state word >= 2^31, or all-zero state */
+#define MRG8G_ERR_CUDA (-3)
+#define MRG8G_ERR_OUT_OF_MEMORY (-4)
+#define MRG8G_ERR_TIMEOUT (-5)
+#define MRG8G_ERR_BUDGET (-6)
+#define MRG8G_ERR_NOT_READY (-7)
+
+/* Uniform scalings.  The reference uses both:
+ *   ORIGINAL  u = S * rnorm          in (0, 1]  original/mrg8.cpp:231-237
+ *   SHIFTED   u = (S - 1) * rnorm    in [0, 1)  cuda/mrg8_cuda.cu:251-252,363,
+ *                                               knl/mrg8.h:353-362
+ * with rnorm = 1.0 / (2^31 - 1) in double.  fp32 outputs are (float) of the
+ * fp64 value (no fp32 path exists in the reference). */
+#define MRG8G_ORIGINAL 0
+#define MRG8G_SHIFTED 1
+
+/* Output kinds for the generic entry points. */
+#define MRG8G_U32 0          /* S in [1, 2^31-1]              */
+#define MRG8G_F64_ORIGINAL 1
+#define MRG8G_F64_SHIFTED 2
+#define MRG8G_F32_ORIGINAL 3
+#define MRG8G_F32_SHIFTED 4
+
+typedef struct mrg8g_generator mrg8g_generator;
+
+/* ---- lifetime, seeding and state ------------------------------------- */
+
+/* Replaces mrg8::mrg8(seed) (original/mrg8.cpp:23-28) and
+ * mrg8_cuda::mrg8_cuda(seed) (cuda/mrg8_cuda.cu:44-63).  Seeds with mcg64ni
+ * (original/mrg8.cpp:180-194; seed 0 means 97531).  The jump tables are
+ * generated on the host, not read from jump_matrix.txt. */
+MRG8G_API int mrg8g_create(uint32_t seed, mrg8g_generator **out);
+
+/* No reference counterpart (the reference classes have no destructor and
+ * leak their device memory, cuda/mrg8_cuda.h:20-45). */
+MRG8G_API int mrg8g_destroy(mrg8g_generator *g);
+
+/* Replaces mrg8::seed_init (original/mrg8.cpp:31-34) and
+ * mrg8_cuda::seed_init (cuda/mrg8_cuda.cu:66-70). */
+MRG8G_API int mrg8g_seed_init(mrg8g_generator *g, uint32_t seed);
+
+/* Replaces mrg8::get_state (original/mrg8.cpp:36-39) and, because the state
+ * is always current here, mrg8_cuda::state_cpy_DtH (cuda/mrg8_cuda.cu:72-79).
+ * st[0] = S[n-1] ... st[7] = S[n-8]. */
+MRG8G_API int mrg8g_get_state(const mrg8g_generator *g, uint32_t st[8]);
+
+/* Replaces mrg8::set_state (original/mrg8.cpp:56-59).  Unlike the reference
+ * CUDA class the new state also governs later device calls.  Words must be
+ * below 2^31 and not all zero (MRG8G_ERR_INVALID_STATE otherwise; the
+ * reference overflows or emits a constant stream on such input). */
+MRG8G_API int mrg8g_set_state(mrg8g_generator *g, const uint32_t st[8]);
+
+/* ---- jump-ahead ------------------------------------------------------- */
+
+/* Replaces mrg8::jump_ahead(uint64_t) (original/mrg8.cpp:125-129): the
+ * handle's state advances by k outputs. */
+MRG8G_API int mrg8g_jump_ahead(mrg8g_generator *g, uint64_t k);
+
+/* Replaces mrg8::jump_ahead(const short[200]) (original/mrg8.cpp:104-122):
+ * bits[i] != 0 sets bit i of a 200-bit jump distance (bits[0] = LSB). */
+MRG8G_API int mrg8g_jump_ahead_bits(mrg8g_generator *g, const short bits[200]);
+
+/* Replaces mrg8::jump_ahead(uint64_t, uint32_t*) (cuda/mrg8.cpp:145-150,
+ * knl/mrg8.h:212-238): writes the state k outputs ahead, handle unchanged. */
+MRG8G_API int mrg8g_jump_state(const mrg8g_generator *g, uint64_t k, uint32_t new_state[8]);
+
+/* Replaces mrg8::jump_ahead(const short[200], uint32_t*) (cuda/mrg8.cpp:127-141). */
+MRG8G_API int mrg8g_jump_state_bits(const mrg8g_generator *g, const short bits[200], uint32_t new_state[8]);
+
+/* ---- bulk generation into device memory ------------------------------- */
+
+/* Replaces mrg8::randint(uint32_t*, int) (original/mrg8.cpp:197-222) for a
+ * device buffer: the next n stream values S in [1, 2^31-1]. */
+MRG8G_API int mrg8g_randint(mrg8g_generator *g, uint32_t *d_out, uint64_t n, void *stream);
+
+/* Replaces mrg8::rand(double*, int) (original/mrg8.cpp:231-239, ORIGINAL)
+ * and mrg8_cuda::mrg8_outer_32 / mrg8_inner (cuda/mrg8_cuda.cu:402-436,
+ * SHIFTED) for a device buffer: the next n uniforms in fp64. */
+MRG8G_API int mrg8g_rand(mrg8g_generator *g, double *d_out, uint64_t n, int scaling, void *stream);
+
+/* fp32 uniforms: (float) of the fp64 value of mrg8g_rand. */
+MRG8G_API int mrg8g_rand_f32(mrg8g_generator *g, float *d_out, uint64_t n, int scaling, void *stream);
+
+/* Generic form of the three above (kind = MRG8G_U32 ... MRG8G_F32_SHIFTED). */
+MRG8G_API int mrg8g_generate(mrg8g_generator *g, void *d_out, uint64_t n, int kind, void *stream);
+
+/* ---- bulk generation into host memory --------------------------------- */
+
+/* The reference's host calls (mrg8::randint / rand / mrg8dnz2, e.g.
+ * original/mrg8.cpp:197-239, cuda/mrg8.cpp:290-339) for a host buffer: the
+ * values are generated on the GPU in chunks through a per-handle device
+ * staging area and copied back; returns when h_out is complete.  Pinned
+ * host memory gives the full copy bandwidth. */
+MRG8G_API int mrg8g_generate_host(mrg8g_generator *g, void *h_out, uint64_t n, int kind);
+
+/* ---- utilities ---------------------------------------------------------- */
+
+/* Uniforms from raw stream values: d_out[i] = scaling of d_in[i], where
+ * d_in[i] must lie in [1, 2^31-1]; kind = MRG8G_F64_* or MRG8G_F32_*.
+ * The conversion of rng_outer_32's epilogue (cuda/mrg8_cuda.cu:363). */
+MRG8G_API int mrg8g_convert(const uint32_t *d_in, void *d_out, uint64_t n, int kind, void *stream);
+
+/* Device batch of jumps: d_states[8 i .. 8 i + 7] = state st advanced by
+ * d_offsets[i] outputs (the per-warp jump prologue of
+ * cuda/mrg8_cuda.cu:313-337, generalised to 64-bit offsets). */
+MRG8G_API int mrg8g_jump_states(const uint32_t st[8], const uint64_t *d_offsets, uint32_t *d_states,
+                      uint64_t count, void *stream);
+
+/* Description of the last error on the calling thread ("" if none). */
+MRG8G_API const char *mrg8g_last_error(void);
+
+/* MRG8G_VERSION of the loaded library. */
+MRG8G_API int mrg8g_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MRG8G_H */

@@ -1,0 +1,90 @@
+"""ctypes binding of libmrg8g.so (the C ABI declared in include/mrg8g.h).
+
+The library is built in-tree by ``mrg8_gb300.build``.  Loading fails loudly
+when it is missing: there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+SUCCESS = 0
+ERR_INVALID_ARGUMENT = -1
+ERR_INVALID_STATE = -2
+ERR_CUDA = -3
+ERR_OUT_OF_MEMORY = -4
+ERR_TIMEOUT = -5
+ERR_BUDGET = -6
+ERR_NOT_READY = -7
+
+ORIGINAL, SHIFTED = 0, 1
+U32, F64_ORIGINAL, F64_SHIFTED, F32_ORIGINAL, F32_SHIFTED = range(5)
+
+_vp = C.c_void_p
+_u32 = C.c_uint32
+_u64 = C.c_uint64
+_int = C.c_int
+
+# name -> (restype, argtypes); every symbol declared in include/mrg8g.h.
+SIGNATURES: dict[str, tuple] = {
+    "mrg8g_version": (_int, []),
+    "mrg8g_last_error": (C.c_char_p, []),
+    "mrg8g_create": (_int, [_u32, _vp]),
+    "mrg8g_destroy": (_int, [_vp]),
+    "mrg8g_seed_init": (_int, [_vp, _u32]),
+    "mrg8g_get_state": (_int, [_vp, _vp]),
+    "mrg8g_set_state": (_int, [_vp, _vp]),
+    "mrg8g_jump_ahead": (_int, [_vp, _u64]),
+    "mrg8g_jump_ahead_bits": (_int, [_vp, _vp]),
+    "mrg8g_jump_state": (_int, [_vp, _u64, _vp]),
+    "mrg8g_jump_state_bits": (_int, [_vp, _vp, _vp]),
+    "mrg8g_randint": (_int, [_vp, _vp, _u64, _vp]),
+    "mrg8g_rand": (_int, [_vp, _vp, _u64, _int, _vp]),
+    "mrg8g_rand_f32": (_int, [_vp, _vp, _u64, _int, _vp]),
+    "mrg8g_generate": (_int, [_vp, _vp, _u64, _int, _vp]),
+    "mrg8g_generate_host": (_int, [_vp, _vp, _u64, _int]),
+    "mrg8g_convert": (_int, [_vp, _vp, _u64, _int, _vp]),
+    "mrg8g_jump_states": (_int, [_vp, _vp, _vp, _u64, _vp]),
+}
+
+
+class MRG8GError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(build_if_missing: bool = False):
+    """Load libmrg8g.so (optionally building it first)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            if not build_if_missing:
+                raise OSError(
+                    f"{LIB_PATH} is missing: build it with `python -m mrg8_gb300.build` "
+                    "(this package has no CPU fallback)")
+            _build.build()
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(rc: int) -> None:
+    if rc != SUCCESS:
+        msg = _lib.mrg8g_last_error().decode(errors="replace") if _lib is not None else ""
+        raise MRG8GError(rc, msg)

@@ -1,0 +1,101 @@
+// mrg8g_device.cuh -- sm_103a device building blocks of the MRG8 kernels.
+//
+// Every kernel translation unit includes this header once; it gets its own
+// copy of the device tables (module globals, uploaded per device by
+// MRG8G_DEFINE_TABLE_UPLOAD) so no kernel ever needs a cudaMalloc.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mrg8g_arith.cuh"
+#include "mrg8g_tables.h"
+
+namespace mrg8g {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+// Output kinds; the numbering is part of the C ABI (include/mrg8g.h).
+enum Kind : int { kU32 = 0, kF64Orig = 1, kF64Shift = 2, kF32Orig = 3, kF32Shift = 4 };
+
+template <int KIND> struct OutOf;
+template <> struct OutOf<kU32> { using T = uint32_t; };
+template <> struct OutOf<kF64Orig> { using T = uint64_t; };
+template <> struct OutOf<kF64Shift> { using T = uint64_t; };
+template <> struct OutOf<kF32Orig> { using T = uint32_t; };
+template <> struct OutOf<kF32Shift> { using T = uint32_t; };
+
+// Output word for the stream value S = x + 1 (x in [0, p-1]).
+template <int KIND>
+__device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t x) {
+    if constexpr (KIND == kU32) return x + 1u;
+    else if constexpr (KIND == kF64Orig) return f64_bits(x, false);
+    else if constexpr (KIND == kF64Shift) return f64_bits(x, true);
+    else if constexpr (KIND == kF32Orig) return f32_bits(x, false);
+    else return f32_bits(x, true);
+}
+
+}  // namespace mrg8g
+
+// Per-translation-unit device tables and their uploader.
+#define MRG8G_DEFINE_TABLE_UPLOAD(fn_name)                                                      \
+    static __device__ __align__(16) uint32_t g_jump[::mrg8g::kDevJump * 64];                    \
+    static __device__ __align__(16) uint32_t g_win[::mrg8g::kWinWords];                         \
+    cudaError_t fn_name() {                                                                    \
+        const ::mrg8g::HostTables& t = ::mrg8g::host_tables();                                 \
+        cudaError_t e = cudaMemcpyToSymbol(g_jump, t.jump, sizeof(g_jump));                    \
+        if (e != cudaSuccess) return e;                                                        \
+        return cudaMemcpyToSymbol(g_win, t.win, sizeof(g_win));                                \
+    }
+
+namespace mrg8g {
+
+// Lane-uniform 8-word state s (canonical or raw words < 2^31) -> A^k s, as
+// canonical residues in [0, p-1], computed by the whole warp: lane l owns
+// row l/4 and columns 2(l%4), 2(l%4)+1 of each A^(2^i) (one 8-byte load),
+// partial sums meet by two xor-shuffles, and the new vector is re-broadcast.
+// Must be called by all 32 lanes with the same s and k.
+__device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uint32_t s[8],
+                                          uint64_t k) {
+    if (k == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int c0 = (lane & 3) << 1;
+    uint32_t a0 = c0 == 0 ? s[0] : c0 == 2 ? s[2] : c0 == 4 ? s[4] : s[6];
+    uint32_t a1 = c0 == 0 ? s[1] : c0 == 2 ? s[3] : c0 == 4 ? s[5] : s[7];
+    uint32_t val = 0;
+    while (k) {
+        const int i = __ffsll((long long)k) - 1;
+        k &= k - 1;
+        const uint2 m = __ldg(reinterpret_cast<const uint2*>(jump + i * 64) + lane);
+        const uint64_t part = (uint64_t)m.x * a0 + (uint64_t)m.y * a1;  // < 2^63
+        uint64_t f = (part & kP) + (part >> 31);                        // < 2^33
+        f += __shfl_xor_sync(kFull, f, 1);
+        f += __shfl_xor_sync(kFull, f, 2);                              // < 2^35
+        val = mod_p64(f);
+        a0 = __shfl_sync(kFull, val, c0 << 2);
+        a1 = __shfl_sync(kFull, val, (c0 << 2) + 4);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[q] = __shfl_sync(kFull, val, q << 2);
+}
+
+// Initial window of a lane for layout V: x[v][j] = S[B + V lane + v + d j] - 1
+// for j = 0..7 (d = 32 V), from the state s taken at stream position B.
+template <int V>
+__device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t s[8],
+                                            int lane, uint32_t (&x)[V][8]) {
+    const uint32_t* w = win + win_offset(layout_index(V));
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        const int o = V * lane + v;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint4* row = reinterpret_cast<const uint4*>(w + (o * 8 + j) * 8);
+            const uint4 r0 = __ldg(row), r1 = __ldg(row + 1);
+            const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+            const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
+            x[v][j] = (S ? S : kP) - 1u;
+        }
+    }
+}
+
+}  // namespace mrg8g

@@ -1,0 +1,35 @@
+// mrg8g_internal.h -- launch interfaces between the C ABI and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mrg8g_tables.h"
+
+namespace mrg8g {
+
+constexpr int kPlainThreads = 128;  // 4 warps per block
+
+// One bulk call: n outputs starting at the stream position of `st`.
+struct PlainArgs {
+    uint32_t st[8];   // state at stream position 0 of the call (raw words)
+    uint64_t n;       // outputs
+    uint64_t head;    // outputs [0, head) written by one lane (alignment)
+    uint64_t tile;    // outputs per warp, a multiple of 32 V
+    void* out;        // device pointer to output element 0
+    LeapCoef lc;      // decimated recurrence of the layout
+};
+
+struct JumpArgs {
+    uint32_t st[8];
+    const uint64_t* offsets;
+    uint32_t* states;
+    uint64_t count;
+};
+
+cudaError_t upload_tables_plain();
+cudaError_t launch_plain(int kind, int V, const PlainArgs& a, int blocks, cudaStream_t st);
+int plain_blocks_per_sm(int kind, int V);
+cudaError_t launch_convert(int kind, const uint32_t* in, void* out, uint64_t n, int blocks, cudaStream_t st);
+cudaError_t launch_jump_states(const JumpArgs& a, int blocks, cudaStream_t st);
+
+}  // namespace mrg8g

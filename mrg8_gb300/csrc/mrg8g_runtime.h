@@ -1,0 +1,30 @@
+// mrg8g_runtime.h -- host runtime helpers shared by the C ABI translation
+// units (errors, per-device setup, launch planning, state bookkeeping).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+
+namespace mrg8g {
+
+struct DeviceInfo;
+
+// Record an error for mrg8g_last_error() and return `code`.
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+// Make the current device ready (tables uploaded, limits queried).
+int ensure_device(int* dev_out, const DeviceInfo** info);
+int device_sms();
+
+int kind_elem_bytes(int kind);
+bool kind_valid(int kind);
+int default_layout_V(int kind);
+int validate_state(const uint32_t st[8]);
+void advance_state(uint32_t st[8], uint64_t n);
+int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, cudaStream_t s, int V);
+
+cudaError_t upload_tables_batch();
+
+}  // namespace mrg8g

@@ -1,0 +1,97 @@
+// check_kernel_math.cpp -- CPU check of the arithmetic the kernels run.
+//
+// Built by tests/test_kernel_math.py with g++ against the library's host
+// sources (mrg8g_tables.cpp and the shared header mrg8g_arith.cuh).
+//
+//   check_kernel_math conv
+//       every v in [1, 2^31-1]: integer fp64/fp32 words == RN(double(v) *
+//       (1.0/(2^31-1))) and (float) of it; plus the SHIFTED zero.
+//   check_kernel_math leap <stream.bin> <s0..s7>
+//       stream.bin holds the oracle's outputs S[0..N) from state s; checks
+//       the window tables (S[B + o + d j] = row . s_B at B = 0) and runs every
+//       layout's decimated recurrence with the kernels' step (mad_wide_s32 +
+//       reduce_acc) over the whole stream; writes the row-major jump table to
+//       stdout as raw u32 for the Python side to compare.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mrg8g_arith.cuh"
+#include "mrg8g_tables.h"
+
+using namespace mrg8g;
+
+static int conv() {
+    const double rnorm = 1.0 / 2147483647.0;
+    unsigned long bad = 0;
+    for (uint64_t v = 1; v <= 2147483647ull; ++v) {
+        const double d = (double)(uint32_t)v * rnorm;
+        uint64_t db;
+        std::memcpy(&db, &d, 8);
+        const float f = (float)d;
+        uint32_t fb;
+        std::memcpy(&fb, &f, 4);
+        if (db != f64_bits_pos((uint32_t)v) || fb != f32_bits_pos((uint32_t)v)) {
+            if (bad++ < 8) std::fprintf(stderr, "mismatch at v=%lu\n", (unsigned long)v);
+        }
+        // SHIFTED uses x = S - 1 = v: the same words; ORIGINAL uses v = x + 1.
+        if (v < 2147483647ull && (f64_bits((uint32_t)v, true) != db || f64_bits((uint32_t)v - 1, false) != db))
+            bad++;
+    }
+    if (f64_bits(0, true) != 0 || f32_bits(0, true) != 0) bad++;
+    std::printf("conv bad=%lu\n", bad);
+    return bad ? 1 : 0;
+}
+
+static int leap(const char* path, const uint32_t s0[8]) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return 2;
+    std::vector<uint32_t> S;
+    uint32_t buf[4096];
+    size_t got;
+    while ((got = std::fread(buf, 4, 4096, f)) > 0) S.insert(S.end(), buf, buf + got);
+    std::fclose(f);
+    const HostTables& t = host_tables();
+    unsigned long bad = 0, checked = 0;
+    for (int li = 0; li < kNumLayouts; ++li) {
+        const int d = layout_stride(li);
+        const uint32_t* w = t.win + win_offset(li);
+        const LeapCoef& lc = t.leap[li];
+        if (S.size() < (size_t)d * 16) return 3;
+        const size_t rows = S.size() / d;
+        for (int o = 0; o < d; ++o) {
+            uint32_t x[8];
+            for (int j = 0; j < 8; ++j) {
+                const uint32_t v = dot8_ref(w + (o * 8 + j) * 8, s0);
+                const uint32_t Sv = v ? v : kP;
+                if (Sv != S[o + (size_t)d * j]) bad++;
+                x[j] = Sv - 1u;
+            }
+            for (size_t j = 8; j < rows; ++j) {
+                uint64_t acc = lc.K;
+                for (int k = 1; k <= 8; ++k) acc = mad_wide_s32(lc.c[k - 1], x[(j - k) & 7], acc);
+                const uint32_t xn = reduce_acc(acc);
+                x[j & 7] = xn;
+                if (xn + 1u != S[o + (size_t)d * j]) {
+                    if (bad++ < 8) std::fprintf(stderr, "leap mismatch d=%d o=%d j=%zu\n", d, o, j);
+                }
+                checked++;
+            }
+        }
+    }
+    std::fwrite(t.jump, 4, sizeof(t.jump) / 4, stdout);
+    std::fprintf(stderr, "leap checked=%lu bad=%lu\n", checked, bad);
+    return bad ? 1 : 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc >= 2 && !std::strcmp(argv[1], "conv")) return conv();
+    if (argc >= 11 && !std::strcmp(argv[1], "leap")) {
+        uint32_t s[8];
+        for (int q = 0; q < 8; ++q) s[q] = (uint32_t)std::strtoul(argv[3 + q], nullptr, 10);
+        return leap(argv[2], s);
+    }
+    std::fprintf(stderr, "usage: check_kernel_math conv | leap <stream.bin> s0..s7\n");
+    return 2;
+}
