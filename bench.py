@@ -202,7 +202,7 @@ def run_gpu(args) -> None:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
-    n = N_PER_RANK
+    n = args.n
     kind = m.F64_SHIFTED
     g = m.MRG8(SEED)
     if rank:
@@ -245,20 +245,24 @@ def run_gpu(args) -> None:
     hbm = float(peaks.get("hbm_gbs", 6800.0))
 
     # fp32 at the same size (secondary line item; not the headline).
-    out32 = torch.empty(n, dtype=torch.float32, device=dev)
-    for _ in range(3):
-        g.set_state(st0)
-        g.rand_f32(out32, scaling=1)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = max(3, args.steps // 2)
-    e0.record(stream)
-    for _ in range(reps):
-        g.set_state(st0)
-        g.rand_f32(out32, scaling=1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    f32_s = e0.elapsed_time(e1) / 1e3 / reps
-    del out32
+    f32 = None
+    if not args.skip_f32:
+        out32 = torch.empty(n, dtype=torch.float32, device=dev)
+        for _ in range(3):
+            g.set_state(st0)
+            g.rand_f32(out32, scaling=1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(3, args.steps // 2)
+        e0.record(stream)
+        for _ in range(reps):
+            g.set_state(st0)
+            g.rand_f32(out32, scaling=1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        f32_s = e0.elapsed_time(e1) / 1e3 / reps
+        del out32
+        f32 = {"value": round(n / f32_s / 1e9, 4), "unit": UNIT, "gbs": round(4.0 * n / f32_s / 1e9, 1),
+               "frac_hbm": round(4.0 * n / f32_s / 1e9 / hbm, 4)}
 
     # End to end through the C ABI with a pinned host buffer.
     e2e = None
@@ -288,8 +292,9 @@ def run_gpu(args) -> None:
 
     # Spot check of this run's output against the oracle (first 2^20 values).
     from oracle.pyoracle import F64_SHIFTED as O_F64S, Oracle
-    ref, _ = Oracle().generate(st0, 1 << 20, O_F64S, nthreads=os.cpu_count() or 8)
-    ok = bool(np.array_equal(out[: 1 << 20].cpu().numpy().view(np.uint64), ref.view(np.uint64)))
+    chk = min(n, 1 << 20)
+    ref, _ = Oracle().generate(st0, chk, O_F64S, nthreads=os.cpu_count() or 8)
+    ok = bool(np.array_equal(out[:chk].cpu().numpy().view(np.uint64), ref.view(np.uint64)))
 
     if rank != 0:
         if pg:
@@ -309,8 +314,7 @@ def run_gpu(args) -> None:
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": f"{peak_src} hbm_gbs (copy)",
                      "traffic": traffic, "algorithmic_bytes_per_launch": 8 * n},
-        "f32": {"value": round(n / f32_s / 1e9, 4), "unit": UNIT, "gbs": round(4.0 * n / f32_s / 1e9, 1),
-                "frac_hbm": round(4.0 * n / f32_s / 1e9 / hbm, 4)},
+        "f32": f32,
         "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": args.steps,
         "parity_spot_check": ok, "wall_s": round(wall, 4),
     }
@@ -327,6 +331,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-f32", action="store_true")
+    ap.add_argument("--n", type=int, default=N_PER_RANK, help="outputs per GPU (profiling of small cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
