@@ -140,7 +140,28 @@ MRG8G_API int mrg8g_generate(mrg8g_generator *g, void *d_out, uint64_t n, int ki
  * host memory gives the full copy bandwidth. */
 MRG8G_API int mrg8g_generate_host(mrg8g_generator *g, void *h_out, uint64_t n, int kind);
 
+/* One instance through the bulk kernel without a handle: the n outputs of
+ * `kind` that follow the first `offset` outputs after state st.  This is the
+ * per-instance path (one launch per generator) that the batch entry points
+ * replace. */
+MRG8G_API int mrg8g_generate_from_state(const uint32_t st[8], uint64_t offset, void *d_out, uint64_t n,
+                                        int kind, void *stream);
+
 /* ---- utilities ---------------------------------------------------------- */
+
+/* st = the state seeded from `seed` by mcg64ni (original/mrg8.cpp:180-194). */
+MRG8G_API int mrg8g_seed_state(uint32_t seed, uint32_t st[8]);
+
+/* Wait for the work queued on `stream` (NULL = legacy default stream).  The
+ * synchronous drop-in methods use it: the reference synchronises the device
+ * after each launch (cuda/mrg8_cuda.cu:409,423). */
+MRG8G_API int mrg8g_stream_sync(void *stream);
+
+/* Launch shape of the bulk kernel for one output kind, process-wide (set by
+ * the autotuner): V = substreams per lane (1, 2 or 4; 0 = default for the
+ * kind) and blocks_per_sm = resident blocks per SM (0 = occupancy maximum). */
+MRG8G_API int mrg8g_tune_plain(int kind, int V, int blocks_per_sm);
+MRG8G_API int mrg8g_get_plain_tuning(int kind, int *V, int *blocks_per_sm);
 
 /* Uniforms from raw stream values: d_out[i] = scaling of d_in[i], where
  * d_in[i] must lie in [1, 2^31-1]; kind = MRG8G_F64_* or MRG8G_F32_*.

@@ -35,8 +35,22 @@ MRG8G_HD uint32_t clz32(uint32_t v) {
 #endif
 }
 
+// 32 x 32 -> 64-bit unsigned multiply-add (one IMAD.WIDE.U32 on the device).
+MRG8G_HD uint64_t mad_wide_u32(uint32_t a, uint32_t b, uint64_t c) {
+#if defined(__CUDA_ARCH__)
+    uint64_t d;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+    return d;
+#else
+    return (uint64_t)a * b + c;
+#endif
+}
+
 // Normalised 53-bit significand m (2^52 <= m <= 2^53) and the biased exponent
-// minus one, for RN(v * rnorm), 1 <= v <= 2^31 - 1.
+// minus one, for RN(v * rnorm), 1 <= v <= 2^31 - 1.  With xn = v << lz
+// (leading one at bit 31) the exact product scaled to [2^52, 2^53) is
+// xn (2^31 + 1) / 2^10, so one multiply-add forms it together with the
+// round-to-nearest-even bias 0x1FF + (bit 10 of xn), and m is that sum >> 10.
 struct Sig53 {
     uint64_t m;
     uint32_t em1;  // biased exponent - 1 (the implicit bit of m adds one)
@@ -45,13 +59,9 @@ struct Sig53 {
 MRG8G_HD Sig53 sig53(uint32_t v) {
     const uint32_t lz = clz32(v);                // 1..31
     const uint32_t xn = v << lz;                 // leading one at bit 31
-    // (v*2^31 + v) << (lz + 1) == xn*2^32 + 2*xn, i.e. hi = xn + 1, lo = 2 xn.
-    const uint64_t w = ((uint64_t)(xn + 1u) << 32) | (uint64_t)(xn << 1);
-    const uint32_t low = (uint32_t)w & 0x7FFu;   // the 11 bits dropped
-    const uint32_t lsb = (xn >> 10) & 1u;        // bit 11 of w
-    const uint32_t up = (low + 0x3FFu + lsb) >> 11;  // round to nearest even
+    const uint32_t lsb = (xn >> 10) & 1u;        // the bit rounded to
     Sig53 r;
-    r.m = (w >> 11) + up;
+    r.m = mad_wide_u32(xn, 0x80000001u, 0x1FFu + lsb) >> 10;
     r.em1 = 1022u - lz;                          // value in [2^-lz, 2^(1-lz))
     return r;
 }

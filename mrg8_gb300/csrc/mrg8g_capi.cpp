@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -94,6 +95,10 @@ bool kind_valid(int kind) { return kind >= MRG8G_U32 && kind <= MRG8G_F32_SHIFTE
 // Substreams per lane: one 16-byte vector of outputs per row.
 int default_layout_V(int kind) { return kind_elem_bytes(kind) == 8 ? 2 : 4; }
 
+// Process-wide launch-shape overrides (mrg8g_tune_plain).
+static std::atomic<int> g_tune_V[5];
+static std::atomic<int> g_tune_bps[5];
+
 int validate_state(const uint32_t st[8]) {
     bool any = false;
     for (int q = 0; q < 8; ++q) {
@@ -128,13 +133,16 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
     const uintptr_t addr = (uintptr_t)d_out;
     if (!d_out) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null output pointer");
     if (addr % elem) return fail(MRG8G_ERR_INVALID_ARGUMENT, "output pointer not aligned to %d bytes", elem);
+    if (V <= 0) V = g_tune_V[kind].load(std::memory_order_relaxed);
     if (V <= 0) V = default_layout_V(kind);
     const int li = layout_index(V);
+    int bps = g_tune_bps[kind].load(std::memory_order_relaxed);
+    if (bps <= 0 || bps > dev->bps[kind][li]) bps = dev->bps[kind][li];
     const uint64_t D = 32ull * V;
     uint64_t head = ((16 - addr % 16) % 16) / elem;
     if (head > n) head = n;
     const uint64_t body = n - head;
-    const uint64_t max_warps = (uint64_t)dev->sms * dev->bps[kind][li] * (kPlainThreads / 32);
+    const uint64_t max_warps = (uint64_t)dev->sms * bps * (kPlainThreads / 32);
     uint64_t tile = (body + max_warps - 1) / max_warps;
     tile = (tile + D - 1) / D * D;
     tile = std::max<uint64_t>(tile, D * 64);
@@ -331,6 +339,46 @@ int mrg8g_generate_host(mrg8g_generator* g, void* h_out, uint64_t n, int kind) {
     for (int i = 0; i < 2; ++i)
         if ((e = cudaStreamSynchronize(g->sstream[i])) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     std::memcpy(g->st, st, sizeof(st));
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_generate_from_state(const uint32_t st[8], uint64_t offset, void* d_out, uint64_t n, int kind,
+                              void* stream) {
+    if (!st) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null state pointer");
+    if (!kind_valid(kind)) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown output kind %d", kind);
+    int rc = validate_state(st);
+    if (rc) return rc;
+    uint32_t s[8];
+    std::memcpy(s, st, sizeof(s));
+    advance_state(s, offset);
+    return launch_plain_call(s, d_out, n, kind, (cudaStream_t)stream, 0);
+}
+
+int mrg8g_seed_state(uint32_t seed, uint32_t st[8]) {
+    if (!st) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null state pointer");
+    mcg64ni(seed, st);
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_stream_sync(void* stream) {
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_tune_plain(int kind, int V, int blocks_per_sm) {
+    if (!kind_valid(kind)) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown output kind %d", kind);
+    if (V != 0 && V != 1 && V != 2 && V != 4) return fail(MRG8G_ERR_INVALID_ARGUMENT, "V must be 0, 1, 2 or 4");
+    if (blocks_per_sm < 0) return fail(MRG8G_ERR_INVALID_ARGUMENT, "negative blocks per SM");
+    g_tune_V[kind].store(V);
+    g_tune_bps[kind].store(blocks_per_sm);
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_get_plain_tuning(int kind, int* V, int* blocks_per_sm) {
+    if (!kind_valid(kind) || !V || !blocks_per_sm) return fail(MRG8G_ERR_INVALID_ARGUMENT, "bad argument");
+    *V = g_tune_V[kind].load();
+    *blocks_per_sm = g_tune_bps[kind].load();
     return MRG8G_SUCCESS;
 }
 

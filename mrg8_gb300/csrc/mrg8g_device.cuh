@@ -79,23 +79,27 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uin
 }
 
 // Initial window of a lane for layout V: x[v][j] = S[B + V lane + v + d j] - 1
-// for j = 0..7 (d = 32 V), from the state s taken at stream position B.
+// for j = 0..7 (d = 32 V), from the state s taken at stream position B.  The
+// 8 V dot products run one at a time (keeping the setup's register peak
+// below the main loop's) through the warp's scratch rows in shared memory,
+// `scratch` holding 8 V * 32 words laid out [slot][lane].
 template <int V>
 __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t s[8],
-                                            int lane, uint32_t (&x)[V][8]) {
+                                            int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
     const uint32_t* w = win + win_offset(layout_index(V));
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        const int o = V * lane + v;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const uint4* row = reinterpret_cast<const uint4*>(w + (o * 8 + j) * 8);
-            const uint4 r0 = __ldg(row), r1 = __ldg(row + 1);
-            const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-            const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
-            x[v][j] = (S ? S : kP) - 1u;
-        }
+#pragma unroll 1
+    for (int i = 0; i < 8 * V; ++i) {
+        const int v = i >> 3, j = i & 7;
+        const uint4* row = reinterpret_cast<const uint4*>(w + ((V * lane + v) * 8 + j) * 8);
+        const uint4 r0 = __ldg(row), r1 = __ldg(row + 1);
+        const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+        const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
+        scratch[i * 32 + lane] = (S ? S : kP) - 1u;
     }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[v][j] = scratch[(v * 8 + j) * 32 + lane];
 }
 
 }  // namespace mrg8g

@@ -18,13 +18,15 @@ namespace mrg8g {
 
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_plain)
 
+// One row of every substream of the lane.  The oldest lag is accumulated
+// first so that only the last multiply-add waits for the previous row.
 template <int V>
 __device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapCoef& lc) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
         uint64_t acc = lc.K;
 #pragma unroll
-        for (int k = 1; k <= 8; ++k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
+        for (int k = 8; k >= 1; --k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
         x[v][u] = reduce_acc(acc);
     }
 }
@@ -100,8 +102,9 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__
     for (int q = 0; q < 8; ++q) s[q] = a.st[q];
     warp_jump(g_jump, s, B);
 
+    __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
     uint32_t x[V][8];
-    lane_window<V>(g_win, s, lane, x);
+    lane_window<V>(g_win, s, lane, scratch[threadIdx.x >> 5], x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
     const uint32_t lane_off = (uint32_t)V * (uint32_t)lane;
