@@ -147,6 +147,52 @@ MRG8G_API int mrg8g_generate_host(mrg8g_generator *g, void *h_out, uint64_t n, i
 MRG8G_API int mrg8g_generate_from_state(const uint32_t st[8], uint64_t offset, void *d_out, uint64_t n,
                                         int kind, void *stream);
 
+/* ---- batches of independent instances ---------------------------------- */
+
+/* One generator instance of a batch: the n outputs of `kind` that follow the
+ * first `offset` outputs after `state` go to the device buffer `out`.  A
+ * batch replaces one mrg8_cuda object and one mrg8_outer_32 launch per
+ * instance (cuda/mrg8_cuda.cu:414-436); every instance's values equal its own
+ * sequential stream. */
+typedef struct mrg8g_instance {
+    uint32_t state[8]; /* as get_state (mrg8g_seed_state for a seed)      */
+    uint64_t offset;   /* outputs skipped before the first one written     */
+    uint64_t n;        /* outputs                                          */
+    void *out;         /* device pointer aligned to the element size       */
+    int32_t kind;      /* MRG8G_U32 ... MRG8G_F32_SHIFTED                   */
+    int32_t reserved;  /* 0                                                */
+} mrg8g_instance;
+
+/* Launch shape of a batch; zero fields take the defaults. */
+typedef struct mrg8g_batch_config {
+    int32_t tile_rows;     /* warp rows per tile, multiple of 8 (512)        */
+    int32_t threads;       /* threads per block, 128 or 256 (128)            */
+    int32_t blocks_per_sm; /* resident blocks per SM cap (0 = occupancy max) */
+    int32_t use_graph;     /* 1: launch through a captured CUDA graph        */
+} mrg8g_batch_config;
+
+typedef struct mrg8g_batch mrg8g_batch;
+
+/* Plan a batch: validates the instances, cuts them into tiles (longest
+ * first) and uploads the descriptors.  cfg may be NULL (defaults, graph on).
+ * No reference counterpart (the reference has one object per stream). */
+MRG8G_API int mrg8g_batch_create(const mrg8g_instance *inst, uint64_t count, const mrg8g_batch_config *cfg,
+                                 mrg8g_batch **out);
+
+/* Enqueue the whole batch on `stream`: one persistent kernel (plus the reset
+ * of its work counter), through the plan's CUDA graph when use_graph = 1.
+ * Launches of one plan must not overlap each other on the device. */
+MRG8G_API int mrg8g_batch_launch(mrg8g_batch *b, void *stream);
+
+/* Time the candidate shapes on this batch (synchronises `stream`), keep the
+ * fastest and report it in *chosen (may be NULL). */
+MRG8G_API int mrg8g_batch_autotune(mrg8g_batch *b, void *stream, mrg8g_batch_config *chosen);
+
+MRG8G_API int mrg8g_batch_get_config(const mrg8g_batch *b, mrg8g_batch_config *cfg);
+MRG8G_API int mrg8g_batch_set_config(mrg8g_batch *b, const mrg8g_batch_config *cfg);
+MRG8G_API int mrg8g_batch_stats(const mrg8g_batch *b, uint64_t *tiles, uint64_t *outputs, uint64_t *bytes);
+MRG8G_API int mrg8g_batch_destroy(mrg8g_batch *b);
+
 /* ---- utilities ---------------------------------------------------------- */
 
 /* st = the state seeded from `seed` by mcg64ni (original/mrg8.cpp:180-194). */

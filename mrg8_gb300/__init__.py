@@ -7,9 +7,10 @@ reference classes.  Build the library with ``python -m mrg8_gb300.build``.
 """
 from ._lib import (F32_ORIGINAL, F32_SHIFTED, F64_ORIGINAL, F64_SHIFTED, ORIGINAL, SHIFTED, U32,
                    MRG8GError, load)
-from .api import MAX_RND, MRG8, MRG8Cuda, P, convert, jump_states
+from .api import MAX_RND, MRG8, Batch, MRG8Cuda, P, convert, generate_from_state, jump_states, seed_state
 
 __all__ = [
-    "MRG8", "MRG8Cuda", "MRG8GError", "load", "convert", "jump_states", "P", "MAX_RND",
+    "MRG8", "MRG8Cuda", "Batch", "MRG8GError", "load", "convert", "jump_states", "seed_state",
+    "generate_from_state", "P", "MAX_RND",
     "ORIGINAL", "SHIFTED", "U32", "F64_ORIGINAL", "F64_SHIFTED", "F32_ORIGINAL", "F32_SHIFTED",
 ]

@@ -55,7 +55,26 @@ SIGNATURES: dict[str, tuple] = {
     "mrg8g_stream_sync": (_int, [_vp]),
     "mrg8g_tune_plain": (_int, [_int, _int, _int]),
     "mrg8g_get_plain_tuning": (_int, [_int, _vp, _vp]),
+    "mrg8g_batch_create": (_int, [_vp, _u64, _vp, _vp]),
+    "mrg8g_batch_launch": (_int, [_vp, _vp]),
+    "mrg8g_batch_autotune": (_int, [_vp, _vp, _vp]),
+    "mrg8g_batch_get_config": (_int, [_vp, _vp]),
+    "mrg8g_batch_set_config": (_int, [_vp, _vp]),
+    "mrg8g_batch_stats": (_int, [_vp, _vp, _vp, _vp]),
+    "mrg8g_batch_destroy": (_int, [_vp]),
 }
+
+
+class Instance(C.Structure):
+    """mrg8g_instance of include/mrg8g.h."""
+    _fields_ = [("state", C.c_uint32 * 8), ("offset", C.c_uint64), ("n", C.c_uint64), ("out", C.c_void_p),
+                ("kind", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchConfig(C.Structure):
+    """mrg8g_batch_config of include/mrg8g.h."""
+    _fields_ = [("tile_rows", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("use_graph", C.c_int32)]
 
 
 class MRG8GError(RuntimeError):

@@ -39,6 +39,8 @@ def _kind(family: str, scaling: int) -> int:
 
 def _target(arr, kind: int, n):
     """(pointer, element count, is_device, stream) for an output array."""
+    if kind not in _KIND_BYTES:
+        raise ValueError(f"unknown output kind {kind}")
     esize = _KIND_BYTES[kind]
     if torch is not None and isinstance(arr, torch.Tensor):
         if not arr.is_contiguous():
@@ -273,3 +275,103 @@ def jump_states(state, d_offsets) -> "torch.Tensor":
         check(lib.mrg8g_jump_states(st.ctypes.data, C.c_void_p(d_offsets.data_ptr()),
                                     C.c_void_p(out.data_ptr()), C.c_uint64(count), C.c_void_p(stream)))
     return out
+
+
+class Batch:
+    """Many independent generator instances in one persistent launch.
+
+    ``instances`` is a sequence of ``(state, offset, out, kind)`` tuples (or
+    dicts with those keys): ``state`` the 8-word state (``seed_state(seed)``
+    for a seed), ``offset`` the outputs skipped first, ``out`` a contiguous
+    CUDA tensor receiving ``out.numel()`` outputs (or ``n`` given explicitly
+    as a fifth tuple item / dict key), ``kind`` one of U32, F64_*, F32_*.
+    Each instance receives exactly the values of its own sequential stream.
+    """
+
+    def __init__(self, instances, tile_rows: int = 0, threads: int = 0, blocks_per_sm: int = 0,
+                 use_graph: bool = True):
+        self._lib = _lib.load()
+        items = []
+        self._keep = []
+        device = None
+        for it in instances:
+            if isinstance(it, dict):
+                state, offset, out, kind, n = it["state"], it.get("offset", 0), it["out"], it["kind"], it.get("n")
+            else:
+                state, offset, out, kind = it[:4]
+                n = it[4] if len(it) > 4 else None
+            ptr, n, dev, _, dv = _target(out, kind, n)
+            if not dev:
+                raise TypeError("batch outputs must be CUDA tensors")
+            device = device or dv
+            inst = _lib.Instance()
+            inst.state[:] = [int(v) for v in _state_arr(state)]
+            inst.offset, inst.n, inst.out, inst.kind, inst.reserved = int(offset), int(n), ptr, int(kind), 0
+            items.append(inst)
+            self._keep.append(out)
+        arr = (_lib.Instance * max(len(items), 1))(*items)
+        cfg = _lib.BatchConfig(tile_rows, threads, blocks_per_sm, 1 if use_graph else 0)
+        self.device = device
+        h = C.c_void_p()
+        with torch.cuda.device(device or torch.cuda.current_device()):
+            check(self._lib.mrg8g_batch_create(arr, C.c_uint64(len(items)), C.byref(cfg), C.byref(h)))
+        self._h = h
+
+    def launch(self, stream=None) -> None:
+        """Enqueue the whole batch (one graph launch) on torch's current
+        stream or the given one."""
+        with torch.cuda.device(self.device or torch.cuda.current_device()):
+            s = (stream or torch.cuda.current_stream()).cuda_stream
+            check(self._lib.mrg8g_batch_launch(self._h, C.c_void_p(s)))
+
+    def autotune(self) -> dict:
+        with torch.cuda.device(self.device or torch.cuda.current_device()):
+            cfg = _lib.BatchConfig()
+            s = torch.cuda.current_stream().cuda_stream
+            check(self._lib.mrg8g_batch_autotune(self._h, C.c_void_p(s), C.byref(cfg)))
+        return {"tile_rows": cfg.tile_rows, "threads": cfg.threads, "blocks_per_sm": cfg.blocks_per_sm,
+                "use_graph": cfg.use_graph}
+
+    @property
+    def config(self) -> dict:
+        cfg = _lib.BatchConfig()
+        check(self._lib.mrg8g_batch_get_config(self._h, C.byref(cfg)))
+        return {"tile_rows": cfg.tile_rows, "threads": cfg.threads, "blocks_per_sm": cfg.blocks_per_sm,
+                "use_graph": cfg.use_graph}
+
+    def stats(self) -> dict:
+        t, o, b = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(self._lib.mrg8g_batch_stats(self._h, C.byref(t), C.byref(o), C.byref(b)))
+        return {"tiles": t.value, "outputs": o.value, "bytes": b.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.mrg8g_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def seed_state(seed: int) -> np.ndarray:
+    """The state mcg64ni seeds from `seed` (original/mrg8.cpp:180-194)."""
+    lib = _lib.load()
+    st = np.zeros(8, dtype=np.uint32)
+    check(lib.mrg8g_seed_state(C.c_uint32(seed & 0xFFFFFFFF), st.ctypes.data))
+    return st
+
+
+def generate_from_state(state, offset: int, out, kind: int, n=None, stream=None) -> None:
+    """One instance through the bulk kernel (the per-instance path)."""
+    lib = _lib.load()
+    ptr, n, dev, s, device = _target(out, kind, n)
+    if not dev:
+        raise TypeError("generate_from_state writes device tensors")
+    st = _state_arr(state)
+    with torch.cuda.device(device):
+        s = (stream.cuda_stream if stream is not None else s)
+        check(lib.mrg8g_generate_from_state(st.ctypes.data, C.c_uint64(offset), C.c_void_p(ptr), C.c_uint64(n),
+                                            kind, C.c_void_p(s)))

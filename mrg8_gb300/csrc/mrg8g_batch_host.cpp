@@ -1,0 +1,311 @@
+// mrg8g_batch_host.cpp -- batches of independent generator instances: the
+// plan (tiles, device descriptors, work-queue counter), its CUDA-graph
+// launch and its autotuner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/mrg8g.h"
+#include "mrg8g_internal.h"
+#include "mrg8g_runtime.h"
+#include "mrg8g_tables.h"
+
+using namespace mrg8g;
+
+struct mrg8g_batch {
+    int dev = -1;
+    std::vector<BatchInst> insts;
+    std::vector<BatchTile> tiles;
+    uint64_t outputs = 0, bytes = 0;
+    mrg8g_batch_config cfg{};
+    int blocks = 0;
+    BatchInst* d_insts = nullptr;
+    BatchTile* d_tiles = nullptr;
+    uint32_t* d_counter = nullptr;
+    size_t d_tiles_cap = 0;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+constexpr int kDefaultTileRows = 512;
+
+void release_graph(mrg8g_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+}
+
+int normalise(mrg8g_batch_config& c) {
+    if (c.tile_rows == 0) c.tile_rows = kDefaultTileRows;
+    if (c.threads == 0) c.threads = 128;
+    if (c.tile_rows < 8 || c.tile_rows > (1 << 20) || (c.tile_rows & 7))
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "tile_rows must be a multiple of 8 in [8, 2^20]");
+    if (c.threads != 128 && c.threads != 256) return fail(MRG8G_ERR_INVALID_ARGUMENT, "threads must be 128 or 256");
+    if (c.blocks_per_sm < 0) return fail(MRG8G_ERR_INVALID_ARGUMENT, "negative blocks_per_sm");
+    if (c.use_graph < 0 || c.use_graph > 1) return fail(MRG8G_ERR_INVALID_ARGUMENT, "use_graph must be 0 or 1");
+    return MRG8G_SUCCESS;
+}
+
+// Tiles of every instance: an unaligned head (fewer outputs than one 16-byte
+// vector) and body tiles of tile_rows rows; ordered by bytes, largest first,
+// so the dynamic queue ends with the smallest pieces.
+void build_tiles(mrg8g_batch* b) {
+    b->tiles.clear();
+    for (uint32_t i = 0; i < (uint32_t)b->insts.size(); ++i) {
+        const BatchInst& in = b->insts[i];
+        if (in.n == 0) continue;
+        const int elem = kind_elem_bytes(in.kind);
+        const uint64_t V = (uint64_t)default_layout_V(in.kind);
+        const uint64_t T = (uint64_t)b->cfg.tile_rows * 32 * V;
+        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
+        if (head > in.n) head = in.n;
+        if (head) b->tiles.push_back({0, i, (uint32_t)head | kTileHead});
+        for (uint64_t s = head; s < in.n; s += T)
+            b->tiles.push_back({s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)});
+    }
+    std::stable_sort(b->tiles.begin(), b->tiles.end(), [&](const BatchTile& x, const BatchTile& y) {
+        const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(b->insts[x.inst].kind);
+        const uint64_t by = (uint64_t)(y.len_flags & ~kTileHead) * kind_elem_bytes(b->insts[y.inst].kind);
+        return bx > by;
+    });
+}
+
+int upload_tiles(mrg8g_batch* b) {
+    cudaError_t e;
+    const size_t need = std::max<size_t>(b->tiles.size(), 1) * sizeof(BatchTile);
+    if (need > b->d_tiles_cap) {
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        if ((e = cudaMalloc(&b->d_tiles, need)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tiles)");
+        b->d_tiles_cap = need;
+    }
+    if (!b->tiles.empty() &&
+        (e = cudaMemcpy(b->d_tiles, b->tiles.data(), b->tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(tiles)");
+    return MRG8G_SUCCESS;
+}
+
+int apply_config(mrg8g_batch* b, const mrg8g_batch_config& c) {
+    mrg8g_batch_config n = c;
+    int rc = normalise(n);
+    if (rc) return rc;
+    const bool retile = n.tile_rows != b->cfg.tile_rows || b->tiles.empty();
+    b->cfg = n;
+    if (retile) {
+        build_tiles(b);
+        if ((rc = upload_tiles(b))) return rc;
+    }
+    const int sms = device_sms();
+    if (!sms) return MRG8G_ERR_CUDA;
+    int bps = batch_blocks_per_sm(n.threads);
+    if (n.blocks_per_sm > 0 && n.blocks_per_sm < bps) bps = n.blocks_per_sm;
+    const uint64_t wpb = (uint64_t)n.threads / 32;
+    const uint64_t want = (b->tiles.size() + wpb - 1) / wpb;
+    b->blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * bps, want));
+    release_graph(b);
+    return MRG8G_SUCCESS;
+}
+
+BatchArgs args_of(const mrg8g_batch* b) {
+    BatchArgs a;
+    a.insts = b->d_insts;
+    a.tiles = b->d_tiles;
+    a.ntiles = (uint32_t)b->tiles.size();
+    a.counter = b->d_counter;
+    for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+    return a;
+}
+
+// Counter reset + persistent kernel, on stream s.
+int enqueue(mrg8g_batch* b, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(counter)");
+    e = launch_batch(args_of(b), b->cfg.threads, b->blocks, s);
+    if (e != cudaSuccess) return cuda_fail(e, "launching the batch kernel");
+    return MRG8G_SUCCESS;
+}
+
+int build_graph(mrg8g_batch* b) {
+    cudaError_t e;
+    if (!b->cap && (e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamCreate(capture)");
+    if ((e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    int rc = enqueue(b, b->cap);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->cap, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return MRG8G_SUCCESS;
+}
+
+void destroy_plan(mrg8g_batch* b) {
+    release_graph(b);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->d_insts) cudaFree(b->d_insts);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->d_counter) cudaFree(b->d_counter);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_batch_config* cfg,
+                       mrg8g_batch** out) {
+    if (!out) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (count && !inst) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null instance array");
+    if (count > 0xFFFFFFFFull) return fail(MRG8G_ERR_INVALID_ARGUMENT, "at most 2^32-1 instances");
+    int dev = 0;
+    int rc = ensure_device(&dev, nullptr);
+    if (rc) return rc;
+    mrg8g_batch* b = new (std::nothrow) mrg8g_batch;
+    if (!b) return fail(MRG8G_ERR_OUT_OF_MEMORY, "host allocation failed");
+    b->dev = dev;
+    b->insts.resize(count);
+    for (uint64_t i = 0; i < count; ++i) {
+        const mrg8g_instance& s = inst[i];
+        if (!kind_valid(s.kind)) {
+            delete b;
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: unknown kind %d", (unsigned long long)i, s.kind);
+        }
+        if ((rc = validate_state(s.state))) {
+            delete b;
+            return rc;
+        }
+        const int elem = kind_elem_bytes(s.kind);
+        if (s.n && (!s.out || (uintptr_t)s.out % elem)) {
+            delete b;
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: null or misaligned output",
+                        (unsigned long long)i);
+        }
+        if (s.n > (1ull << 62) || s.offset > ~0ull - s.n) {
+            delete b;
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: offset + n overflows", (unsigned long long)i);
+        }
+        BatchInst& d = b->insts[i];
+        std::memcpy(d.st, s.state, sizeof(d.st));
+        d.offset = s.offset;
+        d.n = s.n;
+        d.out = s.out;
+        d.kind = s.kind;
+        d.pad = 0;
+        b->outputs += s.n;
+        b->bytes += s.n * elem;
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_insts, std::max<size_t>(count, 1) * sizeof(BatchInst))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_counter, sizeof(uint32_t))) != cudaSuccess) {
+        destroy_plan(b);
+        return cuda_fail(e, "cudaMalloc(batch)");
+    }
+    if (count && (e = cudaMemcpy(b->d_insts, b->insts.data(), count * sizeof(BatchInst), cudaMemcpyHostToDevice)) !=
+                     cudaSuccess) {
+        destroy_plan(b);
+        return cuda_fail(e, "cudaMemcpy(instances)");
+    }
+    mrg8g_batch_config c{};
+    if (cfg) c = *cfg;
+    else c.use_graph = 1;
+    if ((rc = apply_config(b, c))) {
+        destroy_plan(b);
+        return rc;
+    }
+    *out = b;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_launch(mrg8g_batch* b, void* stream) {
+    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
+    if (b->tiles.empty()) return MRG8G_SUCCESS;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!b->cfg.use_graph) return enqueue(b, s);
+    int rc;
+    if (!b->exec && (rc = build_graph(b))) return rc;
+    cudaError_t e = cudaGraphLaunch(b->exec, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_get_config(const mrg8g_batch* b, mrg8g_batch_config* cfg) {
+    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    *cfg = b->cfg;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_set_config(mrg8g_batch* b, const mrg8g_batch_config* cfg) {
+    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    return apply_config(b, *cfg);
+}
+
+int mrg8g_batch_stats(const mrg8g_batch* b, uint64_t* tiles, uint64_t* outputs, uint64_t* bytes) {
+    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
+    if (tiles) *tiles = b->tiles.size();
+    if (outputs) *outputs = b->outputs;
+    if (bytes) *bytes = b->bytes;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chosen) {
+    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
+    if (b->tiles.empty()) {
+        if (chosen) *chosen = b->cfg;
+        return MRG8G_SUCCESS;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess)
+        return cuda_fail(e, "cudaEventCreate");
+    const int use_graph = b->cfg.use_graph;
+    const int rows[] = {128, 256, 512, 1024, 2048};
+    const int threads[] = {128, 256};
+    float best_ms = 1e30f;
+    mrg8g_batch_config best = b->cfg;
+    int rc = MRG8G_SUCCESS;
+    for (int r : rows) {
+        for (int t : threads) {
+            mrg8g_batch_config c{r, t, 0, use_graph};
+            if ((rc = apply_config(b, c))) break;
+            if ((rc = mrg8g_batch_launch(b, s))) break;  // warm-up (and graph build)
+            cudaEventRecord(e0, s);
+            for (int k = 0; k < 3 && !rc; ++k) rc = mrg8g_batch_launch(b, s);
+            cudaEventRecord(e1, s);
+            if ((e = cudaEventSynchronize(e1)) != cudaSuccess) {
+                rc = cuda_fail(e, "cudaEventSynchronize");
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) best_ms = ms, best = c;
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = apply_config(b, best))) return rc;
+    if (chosen) *chosen = best;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_destroy(mrg8g_batch* b) {
+    if (!b) return MRG8G_SUCCESS;
+    destroy_plan(b);
+    return MRG8G_SUCCESS;
+}
+
+}  // extern "C"

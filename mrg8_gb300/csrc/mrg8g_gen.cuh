@@ -1,0 +1,119 @@
+// mrg8g_gen.cuh -- the warp-level generation routine shared by the bulk
+// kernel (mrg8g_plain.cu) and the batch kernel (mrg8g_batch.cu).
+//
+// A warp that holds the stream state s at output position B (lane-uniform)
+// writes the `len` outputs B .. B+len-1 to out[0 .. len): lane l owns the V
+// interleaved decimated substreams at positions B + V l + v + 32 V j, whose
+// first eight values come from the window tables and whose later values come
+// from the order-8 decimated recurrence (8 multiply-adds per output, no
+// communication), and row j of the warp is one contiguous 32 V-element run
+// written with 16-byte vector stores.
+#pragma once
+#include "mrg8g_device.cuh"
+
+namespace mrg8g {
+
+// One row of every substream of the lane.  The oldest lag is accumulated
+// first so that only the last multiply-add waits for the previous row.
+template <int V>
+__device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapCoef& lc) {
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        uint64_t acc = lc.K;
+#pragma unroll
+        for (int k = 8; k >= 1; --k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
+        x[v][u] = reduce_acc(acc);
+    }
+}
+
+// Store slot u of every substream of the lane as V consecutive elements at p.
+template <int V, int KIND>
+__device__ __forceinline__ void store_vec(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u) {
+    using T = typename OutOf<KIND>::T;
+    if constexpr (sizeof(T) == 8) {
+        if constexpr (V == 1) {
+            p[0] = convert<KIND>(x[0][u]);
+        } else {
+#pragma unroll
+            for (int h = 0; h < V; h += 2)
+                *reinterpret_cast<ulonglong2*>(p + h) =
+                    make_ulonglong2(convert<KIND>(x[h][u]), convert<KIND>(x[h + 1][u]));
+        }
+    } else {
+        if constexpr (V == 1) {
+            p[0] = convert<KIND>(x[0][u]);
+        } else if constexpr (V == 2) {
+            *reinterpret_cast<uint2*>(p) = make_uint2(convert<KIND>(x[0][u]), convert<KIND>(x[1][u]));
+        } else {
+            *reinterpret_cast<uint4*>(p) = make_uint4(convert<KIND>(x[0][u]), convert<KIND>(x[1][u]),
+                                                      convert<KIND>(x[2][u]), convert<KIND>(x[3][u]));
+        }
+    }
+}
+
+// Row `row` of the run, checked element by element against its length.
+template <int V, int KIND>
+__device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u,
+                                              uint64_t row, uint64_t full, uint64_t len, uint32_t lane_off) {
+    constexpr uint32_t D = 32 * V;
+    if (row < full) {
+        store_vec<V, KIND>(p + row * D, x, u);
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            if (row * D + lane_off + v < len) p[row * D + v] = convert<KIND>(x[v][u]);
+    }
+}
+
+// The run of `len` outputs from state s (see the file comment).  `out` must
+// be 16-byte aligned when V > 1; `scratch` is the warp's 8 V * 32-word area.
+template <int V, int KIND>
+__device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, const uint32_t s[8],
+                                              typename OutOf<KIND>::T* out, uint64_t len, const LeapCoef& lc,
+                                              uint32_t* scratch) {
+    using T = typename OutOf<KIND>::T;
+    constexpr uint32_t D = 32 * V;
+    const int lane = threadIdx.x & 31;
+    uint32_t x[V][8];
+    lane_window<V>(win, s, lane, scratch, x);
+
+    const uint64_t rows = (len + D - 1) / D, full = len / D;
+    const uint32_t lane_off = (uint32_t)V * (uint32_t)lane;
+    T* const p = out + lane_off;
+
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+        if ((uint64_t)u < rows) store_checked<V, KIND>(p, x, u, (uint64_t)u, full, len, lane_off);
+
+    uint64_t m = 8;
+    for (; m + 8 <= full; m += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            leap_row<V>(x, u, lc);
+            store_vec<V, KIND>(p + (m + u) * D, x, u);
+        }
+    }
+    if (m < rows) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            leap_row<V>(x, u, lc);
+            if (m + u < rows) store_checked<V, KIND>(p, x, u, m + u, full, len, lane_off);
+        }
+    }
+}
+
+// `count` (< V in practice) outputs from state s, one lane, sequentially;
+// the state is advanced.  Used for unaligned heads.
+template <int KIND>
+__device__ __forceinline__ void lane_sequential(const uint32_t* __restrict__ coef, uint32_t st[8],
+                                                typename OutOf<KIND>::T* out, uint64_t count) {
+    for (uint64_t i = 0; i < count; ++i) {
+        const uint32_t S = dot8_ref(coef, st);
+#pragma unroll
+        for (int q = 7; q > 0; --q) st[q] = st[q - 1];
+        st[0] = S;
+        out[i] = convert<KIND>(S - 1u);
+    }
+}
+
+}  // namespace mrg8g

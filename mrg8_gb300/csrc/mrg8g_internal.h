@@ -26,7 +26,39 @@ struct JumpArgs {
     uint64_t count;
 };
 
+// ---- batches of independent instances
+
+// Device copy of one instance (mrg8g_instance of the C ABI).
+struct BatchInst {
+    uint32_t st[8];
+    uint64_t offset;
+    uint64_t n;
+    void* out;
+    int32_t kind;
+    int32_t pad;
+};
+
+// One unit of work: outputs [start, start + len) of instance `inst`.  Bit 31
+// of len_flags marks an unaligned head (fewer outputs than one vector),
+// written sequentially by one lane.
+constexpr uint32_t kTileHead = 0x80000000u;
+struct BatchTile {
+    uint64_t start;
+    uint32_t inst;
+    uint32_t len_flags;
+};
+
+struct BatchArgs {
+    const BatchInst* insts;
+    const BatchTile* tiles;
+    uint32_t ntiles;
+    uint32_t* counter;  // work-queue position, zero before each launch
+    LeapCoef leap[kNumLayouts];
+};
+
 cudaError_t upload_tables_plain();
+cudaError_t launch_batch(const BatchArgs& a, int threads, int blocks, cudaStream_t st);
+int batch_blocks_per_sm(int threads);
 cudaError_t launch_plain(int kind, int V, const PlainArgs& a, int blocks, cudaStream_t st);
 int plain_blocks_per_sm(int kind, int V);
 cudaError_t launch_convert(int kind, const uint32_t* in, void* out, uint64_t n, int blocks, cudaStream_t st);

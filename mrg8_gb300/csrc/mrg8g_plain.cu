@@ -12,69 +12,17 @@
 // shuffles and no shared memory, and every row j of the warp is one
 // contiguous 32 V-element run written with 16-byte vector stores.
 #include "mrg8g_device.cuh"
+#include "mrg8g_gen.cuh"
 #include "mrg8g_internal.h"
 
 namespace mrg8g {
 
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_plain)
 
-// One row of every substream of the lane.  The oldest lag is accumulated
-// first so that only the last multiply-add waits for the previous row.
-template <int V>
-__device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapCoef& lc) {
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        uint64_t acc = lc.K;
-#pragma unroll
-        for (int k = 8; k >= 1; --k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
-        x[v][u] = reduce_acc(acc);
-    }
-}
-
-// Store slot u of every substream of the lane as one vector (V consecutive
-// elements at p).
-template <int V, int KIND>
-__device__ __forceinline__ void store_vec(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u) {
-    using T = typename OutOf<KIND>::T;
-    if constexpr (sizeof(T) == 8) {
-        if constexpr (V == 1) {
-            p[0] = convert<KIND>(x[0][u]);
-        } else {
-#pragma unroll
-            for (int h = 0; h < V; h += 2)
-                *reinterpret_cast<ulonglong2*>(p + h) =
-                    make_ulonglong2(convert<KIND>(x[h][u]), convert<KIND>(x[h + 1][u]));
-        }
-    } else {
-        if constexpr (V == 1) {
-            p[0] = convert<KIND>(x[0][u]);
-        } else if constexpr (V == 2) {
-            *reinterpret_cast<uint2*>(p) = make_uint2(convert<KIND>(x[0][u]), convert<KIND>(x[1][u]));
-        } else {
-            *reinterpret_cast<uint4*>(p) = make_uint4(convert<KIND>(x[0][u]), convert<KIND>(x[1][u]),
-                                                      convert<KIND>(x[2][u]), convert<KIND>(x[3][u]));
-        }
-    }
-}
-
-// Row `row` of the tile, checked against the tile length.
-template <int V, int KIND>
-__device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u,
-                                              uint64_t row, uint64_t full, uint64_t len, uint32_t lane_off) {
-    constexpr uint32_t D = 32 * V;
-    if (row < full) {
-        store_vec<V, KIND>(p + row * D, x, u);
-    } else {
-#pragma unroll
-        for (int v = 0; v < V; ++v)
-            if (row * D + lane_off + v < len) p[row * D + v] = convert<KIND>(x[v][u]);
-    }
-}
-
 template <int V, int KIND>
 __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__ PlainArgs a) {
     using T = typename OutOf<KIND>::T;
-    constexpr uint32_t D = 32 * V;
+    __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
     T* const out = static_cast<T*>(a.out);
     const int lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -84,51 +32,16 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__
         uint32_t st[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) st[q] = a.st[q];
-        for (uint64_t i = 0; i < a.head; ++i) {
-            const uint32_t S = dot8_ref(g_jump, st);  // row 0 of A = coefficients
-#pragma unroll
-            for (int q = 7; q > 0; --q) st[q] = st[q - 1];
-            st[0] = S;
-            out[i] = convert<KIND>(S - 1u);
-        }
+        lane_sequential<KIND>(g_jump, st, out, a.head);  // row 0 of A = coefficients
     }
 
     const uint64_t B = a.head + warp * a.tile;
     if (B >= a.n) return;
-    const uint64_t len = min(a.tile, a.n - B);
-
     uint32_t s[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = a.st[q];
     warp_jump(g_jump, s, B);
-
-    __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
-    uint32_t x[V][8];
-    lane_window<V>(g_win, s, lane, scratch[threadIdx.x >> 5], x);
-
-    const uint64_t rows = (len + D - 1) / D, full = len / D;
-    const uint32_t lane_off = (uint32_t)V * (uint32_t)lane;
-    T* const p = out + B + lane_off;
-
-#pragma unroll
-    for (int u = 0; u < 8; ++u)
-        if ((uint64_t)u < rows) store_checked<V, KIND>(p, x, u, (uint64_t)u, full, len, lane_off);
-
-    uint64_t m = 8;
-    for (; m + 8 <= full; m += 8) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            leap_row<V>(x, u, a.lc);
-            store_vec<V, KIND>(p + (m + u) * D, x, u);
-        }
-    }
-    if (m < rows) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            leap_row<V>(x, u, a.lc);
-            if (m + u < rows) store_checked<V, KIND>(p, x, u, m + u, full, len, lane_off);
-        }
-    }
+    warp_generate<V, KIND>(g_win, s, out + B, min(a.tile, a.n - B), a.lc, scratch[threadIdx.x >> 5]);
 }
 
 // Uniforms from raw stream integers S in [1, p] (grid-stride).

@@ -1,0 +1,154 @@
+"""The batch path (one persistent, graph-captured launch for many independent
+instances) against the oracle and against the per-instance bulk path."""
+import numpy as np
+import pytest
+
+from mrg8_helpers import P
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+KINDS = [po.U32, po.F64_ORIGINAL, po.F64_SHIFTED, po.F32_ORIGINAL, po.F32_SHIFTED]
+ELEM = {po.U32: 4, po.F64_ORIGINAL: 8, po.F64_SHIFTED: 8, po.F32_ORIGINAL: 4, po.F32_SHIFTED: 4}
+
+
+def tdt(kind):
+    import torch
+    if kind == po.U32:
+        return torch.int32
+    return torch.float64 if ELEM[kind] == 8 else torch.float32
+
+
+def as_bytes(t):
+    return t.detach().cpu().numpy().view(np.uint8)
+
+
+def expected(oracle, state, offset, n, kind):
+    st = oracle.jump_matvec(state, offset) if offset else np.asarray(state, dtype=np.uint32)
+    if offset and offset < 8:
+        st = np.asarray(state, dtype=np.uint32)
+        _, st = oracle.randint(st, offset)
+    out, _ = oracle.generate(st, n, kind, nthreads=4)
+    return out
+
+
+def make_instances(cuda, rng, count, max_log2, offsets=True):
+    import torch
+    import mrg8_gb300 as m
+    insts, meta = [], []
+    for i in range(count):
+        kind = KINDS[int(rng.integers(0, 5))]
+        n = int(2 ** rng.uniform(0, max_log2)) if i % 7 else int(rng.choice([0, 1, 2, 3, 5, 7, 8, 9, 31, 129]))
+        off = 0
+        if offsets and i % 3 == 0:
+            off = int(rng.integers(0, 2**63)) if i % 2 else int(rng.integers(0, 10))
+        lead = int(rng.integers(0, 4))
+        buf = torch.full((n + lead + 3,), -5, dtype=tdt(kind), device=cuda)
+        seed = int(rng.integers(0, 2**32))
+        st = m.seed_state(seed)
+        insts.append((st, off, buf[lead:lead + n], kind))
+        meta.append((st, off, n, kind, buf, lead))
+    return insts, meta
+
+
+def check_canaries(meta):
+    import torch
+    for st, off, n, kind, buf, lead in meta:
+        host = buf.cpu()
+        fill = torch.full((1,), -5, dtype=buf.dtype)
+        assert bool((host[:lead] == fill).all()) and bool((host[lead + n:] == fill).all())
+
+
+def test_batch_matches_oracle(cuda, oracle):
+    import torch
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(4)
+    insts, meta = make_instances(cuda, rng, 160, 17)
+    b = m.Batch(insts)
+    b.launch()
+    torch.cuda.synchronize()
+    for (st, off, n, kind, buf, lead), (_, _, view, _) in zip(meta, insts):
+        want = expected(oracle, st, off, n, kind)
+        assert np.array_equal(as_bytes(view), want.view(np.uint8)), (off, n, kind, lead)
+    check_canaries(meta)
+    st = b.stats()
+    assert st["outputs"] == sum(x[2] for x in meta)
+
+
+def test_batch_relaunch_autotune_and_plain_launch_agree(cuda, oracle):
+    import torch
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(9)
+    insts, meta = make_instances(cuda, rng, 60, 19)
+    b = m.Batch(insts)
+    b.launch()
+    torch.cuda.synchronize()
+    first = [as_bytes(v).copy() for (_, _, v, _) in insts]
+    for (_, _, v, _) in insts:
+        v.zero_()
+    b.launch()
+    b.launch()
+    torch.cuda.synchronize()
+    assert all(np.array_equal(as_bytes(v), f) for (_, _, v, _), f in zip(insts, first))
+    cfg = b.autotune()
+    assert cfg["tile_rows"] in (128, 256, 512, 1024, 2048)
+    for (_, _, v, _) in insts:
+        v.zero_()
+    b.launch()
+    torch.cuda.synchronize()
+    assert all(np.array_equal(as_bytes(v), f) for (_, _, v, _), f in zip(insts, first))
+    nog = m.Batch(insts, tile_rows=64, threads=256, use_graph=False)
+    for (_, _, v, _) in insts:
+        v.zero_()
+    nog.launch()
+    torch.cuda.synchronize()
+    assert all(np.array_equal(as_bytes(v), f) for (_, _, v, _), f in zip(insts, first))
+    # the per-instance bulk path gives the same values
+    for (st, off, v, kind), f in zip(insts, first):
+        v.zero_()
+        m.generate_from_state(st, off, v, kind)
+    torch.cuda.synchronize()
+    assert all(np.array_equal(as_bytes(v), f) for (_, _, v, _), f in zip(insts, first))
+    check_canaries(meta)
+
+
+def test_config4_shape_small(cuda, oracle):
+    """Config 4's distribution at reduced scale: distinct seeds, lengths
+    log-uniform in [1, 2^18], dtypes mixed uniformly; every instance equal to
+    its own sequential stream."""
+    import torch
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(2024)
+    insts = []
+    for i in range(1500):
+        kind = [po.F64_SHIFTED, po.F32_SHIFTED, po.U32][int(rng.integers(0, 3))]
+        n = max(1, int(2 ** rng.uniform(0, 18)))
+        out = torch.empty(n, dtype=tdt(kind), device=cuda)
+        insts.append((m.seed_state(i * 2654435761 % 2**32), 0, out, kind))
+    b = m.Batch(insts)
+    b.autotune()
+    for (_, _, v, _) in insts:
+        v.fill_(0)
+    b.launch()
+    torch.cuda.synchronize()
+    for j in list(range(0, 1500, 37)) + [1499]:
+        st, _, v, kind = insts[j]
+        want, _ = oracle.generate(st, v.numel(), kind, nthreads=4)
+        assert np.array_equal(as_bytes(v), want.view(np.uint8)), j
+
+
+def test_batch_edge_cases_and_errors(cuda):
+    import torch
+    import mrg8_gb300 as m
+    empty = m.Batch([])
+    empty.launch()
+    z = torch.empty(0, dtype=torch.float64, device=cuda)
+    m.Batch([(m.seed_state(1), 0, z, po.F64_SHIFTED)]).launch()
+    buf = torch.empty(16, dtype=torch.float64, device=cuda)
+    with pytest.raises(ValueError):
+        m.Batch([(m.seed_state(1), 0, buf, 9)])
+    with pytest.raises(m.MRG8GError):
+        m.Batch([([0] * 8, 0, buf, po.F64_SHIFTED)])
+    with pytest.raises(m.MRG8GError):
+        m.Batch([(m.seed_state(1), 2**64 - 5, buf, po.F64_SHIFTED)])
+    torch.cuda.synchronize()
