@@ -46,50 +46,53 @@ MRG8G_HD uint64_t mad_wide_u32(uint32_t a, uint32_t b, uint64_t c) {
 #endif
 }
 
-// Normalised 53-bit significand m (2^52 <= m <= 2^53) and the biased exponent
-// minus one, for RN(v * rnorm), 1 <= v <= 2^31 - 1.  With xn = v << lz
-// (leading one at bit 31) the exact product scaled to [2^52, 2^53) is
-// xn (2^31 + 1) / 2^10, so one multiply-add forms it together with the
-// round-to-nearest-even bias 0x1FF + (bit 10 of xn), and m is that sum >> 10.
-struct Sig53 {
-    uint64_t m;
-    uint32_t em1;  // biased exponent - 1 (the implicit bit of m adds one)
-};
-
-MRG8G_HD Sig53 sig53(uint32_t v) {
-    const uint32_t lz = clz32(v);                // 1..31
-    const uint32_t xn = v << lz;                 // leading one at bit 31
-    const uint32_t lsb = (xn >> 10) & 1u;        // the bit rounded to
-    Sig53 r;
-    r.m = mad_wide_u32(xn, 0x80000001u, 0x1FFu + lsb) >> 10;
-    r.em1 = 1022u - lz;                          // value in [2^-lz, 2^(1-lz))
-    return r;
+// Left shift that yields 0 for a shift count of 32 (PTX shl clamps).
+MRG8G_HD uint32_t shl_clamp(uint32_t a, uint32_t s) {
+#if defined(__CUDA_ARCH__)
+    uint32_t d;
+    asm("shl.b32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(s));
+    return d;
+#else
+    return s >= 32 ? 0u : a << s;
+#endif
 }
 
-// IEEE-754 bits of RN(v * rnorm) for 1 <= v <= 2^31 - 1.
-MRG8G_HD uint64_t f64_bits_pos(uint32_t v) {
-    const Sig53 s = sig53(v);
-    return ((uint64_t)s.em1 << 52) + s.m;  // m == 2^53 carries into the exponent
+// IEEE-754 bits of RN(v * rnorm) for 0 <= v <= 2^31 - 1 (v = 0 gives +0).
+// With lz = clz(v) and xn = v << lz (leading one at bit 31), the exact
+// product scaled to [2^52, 2^53) is xn (2^31 + 1) / 2^10, so one multiply-add
+// forms it together with the round-to-nearest-even bias 0x1FF + bit 10 of xn;
+// its high word >> 10 plus the exponent field gives the high word of the
+// result (at most 0x3FF00000).  P_hi >= 2^30 for v >= 1 and P_hi = 0 for
+// v = 0, so min(high word, P_hi) maps v = 0 to +0 and changes nothing else.
+MRG8G_HD uint64_t f64_bits_of(uint32_t v) {
+    const uint32_t lz = clz32(v);
+    const uint32_t xn = shl_clamp(v, lz);
+    const uint32_t bias = 0x1FFu + ((xn >> 10) & 1u);
+    const uint64_t P = mad_wide_u32(xn, 0x80000001u, bias);
+    const uint32_t phi = (uint32_t)(P >> 32);
+    const uint32_t lo = (uint32_t)(P >> 10);
+    uint32_t hi = (phi >> 10) + ((1022u - lz) << 20);
+    hi = hi < phi ? hi : phi;
+    return ((uint64_t)hi << 32) | lo;
 }
 
-// IEEE-754 bits of (float)RN(v * rnorm) for 1 <= v <= 2^31 - 1.
-MRG8G_HD uint32_t f32_bits_pos(uint32_t v) {
-    const Sig53 s = sig53(v);
-    const uint32_t lsb = (uint32_t)(s.m >> 29) & 1u;
-    const uint32_t m24 = (uint32_t)((s.m + 0x0FFFFFFFull + lsb) >> 29);  // 2^23..2^24
-    return ((s.em1 - 896u) << 23) + m24;
+// IEEE-754 bits of (float)RN(v * rnorm) for 0 <= v <= 2^31 - 1.  A single
+// round-to-nearest-even of the exact product to 24 bits is
+// ((xn >> 1) + 0x40) >> 7 (xn is even and the halfway case cannot occur);
+// it equals the double rounding through fp64 for every v except
+// v = 0x7FFFFFBF, where the fp64 value lands on a halfway point and rounds up
+// once more.  v = 0 gives +0 through min(., xn).
+MRG8G_HD uint32_t f32_bits_of(uint32_t v) {
+    const uint32_t lz = clz32(v);
+    const uint32_t xn = shl_clamp(v, lz);
+    const uint32_t m24 = ((xn >> 1) + 0x40u) >> 7;
+    uint32_t bits = ((126u - lz) << 23) + m24 + (v == 0x7FFFFFBFu ? 1u : 0u);
+    return bits < xn ? bits : xn;
 }
 
 // x is the stream value minus one, 0 <= x <= p - 1 (S = x + 1 in [1, p]).
-MRG8G_HD uint64_t f64_bits(uint32_t x, bool shifted) {
-    if (shifted) return x ? f64_bits_pos(x) : 0ull;
-    return f64_bits_pos(x + 1u);
-}
-
-MRG8G_HD uint32_t f32_bits(uint32_t x, bool shifted) {
-    if (shifted) return x ? f32_bits_pos(x) : 0u;
-    return f32_bits_pos(x + 1u);
-}
+MRG8G_HD uint64_t f64_bits(uint32_t x, bool shifted) { return f64_bits_of(shifted ? x : x + 1u); }
+MRG8G_HD uint32_t f32_bits(uint32_t x, bool shifted) { return f32_bits_of(shifted ? x : x + 1u); }
 
 // ------------------------------------------------------------ modular math
 
@@ -115,11 +118,13 @@ MRG8G_HD uint32_t mod_p64(uint64_t v) {
     return r >= kP ? r - kP : r;
 }
 
-// One decimated-recurrence step: acc = K + sum_k c_k x_{j-k} in [1, 2^64)
-// (signed 32x32 -> 64-bit multiply-adds, wrapping mod 2^64), then a Mersenne
-// reduction to x_j = S_j - 1 in [0, p-1]:
-//   acc = H 2^32 + L == 2H + L (mod p);  s = L + 2H < 3 * 2^32;
-//   t = (s & p) + (s >> 31) in [1, p + 5];  x = t - 1, minus p when >= p.
+// One decimated-recurrence step.  The multiply-adds form
+// a = K1 + sum_k c_k x_{j-k} in [0, 2^64 - 1) with a == S_j - 1 (mod p)
+// (signed 32x32 -> 64-bit products, wrapping mod 2^64; K1 is chosen on the
+// host).  The reduction to x_j = S_j - 1 in [0, p-1]:
+//   a = H 2^32 + L == 2H + L (mod p);  s = 2H + L < 3 * 2^32  (one mad.wide);
+//   y = (s mod 2^31) + (s >> 31) = s_lo - (s >> 31) p  in [0, p + 5];
+//   x = y, or y - p when y >= p.
 MRG8G_HD uint64_t mad_wide_s32(int32_t a, uint32_t b, uint64_t c) {
 #if defined(__CUDA_ARCH__)
     uint64_t d;
@@ -130,13 +135,12 @@ MRG8G_HD uint64_t mad_wide_s32(int32_t a, uint32_t b, uint64_t c) {
 #endif
 }
 
-MRG8G_HD uint32_t reduce_acc(uint64_t acc) {
-    const uint32_t L = (uint32_t)acc, H = (uint32_t)(acc >> 32);
-    const uint64_t s = (uint64_t)L + ((uint64_t)H << 1);
-    const uint32_t t = ((uint32_t)s & kP) + (uint32_t)(s >> 31);
-    const uint32_t x = t - 1u;
-    const uint32_t y = x - kP;
-    return x < y ? x : y;
+MRG8G_HD uint32_t reduce_acc(uint64_t a) {
+    const uint64_t s = mad_wide_u32((uint32_t)(a >> 32), 2u, (uint32_t)a);
+    const uint32_t q = (uint32_t)(s >> 31);
+    const uint32_t y = (uint32_t)s - q * kP;
+    const uint32_t z = y - kP;
+    return y < z ? y : z;
 }
 
 // Residue in [0, p-1] -> stream representative in [1, p].

@@ -19,7 +19,7 @@ template <int V>
 __device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapCoef& lc) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-        uint64_t acc = lc.K;
+        uint64_t acc = lc.K1;
 #pragma unroll
         for (int k = 8; k >= 1; --k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
         x[v][u] = reduce_acc(acc);

@@ -108,13 +108,15 @@ static LeapCoef make_leap(const uint32_t beta[8]) {
         if (c < 0) negsum += (unsigned __int128)(-c);
         else possum += (unsigned __int128)c;
     }
-    const uint64_t cmod = (uint64_t)(((csum % (int64_t)kP) + (int64_t)kP) % (int64_t)kP);
-    const unsigned __int128 base = negsum * (kP - 1) + 1;  // keeps acc >= 1
+    // K1 == sum c_k - 1 (mod p), the smallest such value >= negsum (p - 1), so
+    // that K1 + sum c_k x_k (x_k in [0, p-1]) stays in [0, 2^64 - 1).
+    const uint64_t cmod = (uint64_t)(((csum - 1) % (int64_t)kP + (int64_t)kP) % (int64_t)kP);
+    const unsigned __int128 base = negsum * (kP - 1);
     const uint64_t bmod = (uint64_t)(base % kP);
-    const unsigned __int128 K = base + (cmod + kP - bmod) % kP;
-    const unsigned __int128 top = K + possum * (kP - 1);
-    if (top >> 64) throw std::runtime_error("mrg8g: accumulator range exceeds 64 bits");
-    lc.K = (uint64_t)K;
+    const unsigned __int128 K1 = base + (cmod + kP - bmod) % kP;
+    const unsigned __int128 top = K1 + possum * (kP - 1);
+    if (top >= ~(unsigned __int128)0 >> 64) throw std::runtime_error("mrg8g: accumulator range exceeds 64 bits");
+    lc.K1 = (uint64_t)K1;
     return lc;
 }
 

@@ -35,12 +35,12 @@ constexpr int kWinWords = (32 + 64 + 128) * 64;
 // (Cayley-Hamilton).  For the kernels the coefficients are stored signed,
 // c_k = beta_k or beta_k - p (|c_k| < 2^30), and the kernels keep the lagged
 // values as x = S - 1 in [0, p-1]; then
-//     acc = K + sum_k c_k x_{j-k}
-// lies in [1, 2^64) and acc == S_j (mod p), where K == sum_k c_k (mod p) is
-// the smallest such constant keeping acc >= 1.
+//     a = K1 + sum_k c_k x_{j-k}
+// lies in [0, 2^64 - 1) and a == S_j - 1 (mod p), where K1 == sum_k c_k - 1
+// (mod p) is the smallest such constant keeping a >= 0.
 struct LeapCoef {
     int32_t c[8];
-    uint64_t K;
+    uint64_t K1;
 };
 
 struct HostTables {

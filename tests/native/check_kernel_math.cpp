@@ -32,12 +32,13 @@ static int conv() {
         const float f = (float)d;
         uint32_t fb;
         std::memcpy(&fb, &f, 4);
-        if (db != f64_bits_pos((uint32_t)v) || fb != f32_bits_pos((uint32_t)v)) {
+        if (db != f64_bits_of((uint32_t)v) || fb != f32_bits_of((uint32_t)v)) {
             if (bad++ < 8) std::fprintf(stderr, "mismatch at v=%lu\n", (unsigned long)v);
         }
-        // SHIFTED uses x = S - 1 = v: the same words; ORIGINAL uses v = x + 1.
-        if (v < 2147483647ull && (f64_bits((uint32_t)v, true) != db || f64_bits((uint32_t)v - 1, false) != db))
+        // SHIFTED converts x = S - 1 = v; ORIGINAL converts v = x + 1.
+        if (v < 2147483647ull && (f64_bits((uint32_t)v, true) != db || f32_bits((uint32_t)v, true) != fb))
             bad++;
+        if (f64_bits((uint32_t)v - 1, false) != db || f32_bits((uint32_t)v - 1, false) != fb) bad++;
     }
     if (f64_bits(0, true) != 0 || f32_bits(0, true) != 0) bad++;
     std::printf("conv bad=%lu\n", bad);
@@ -69,7 +70,7 @@ static int leap(const char* path, const uint32_t s0[8]) {
                 x[j] = Sv - 1u;
             }
             for (size_t j = 8; j < rows; ++j) {
-                uint64_t acc = lc.K;
+                uint64_t acc = lc.K1;
                 for (int k = 1; k <= 8; ++k) acc = mad_wide_s32(lc.c[k - 1], x[(j - k) & 7], acc);
                 const uint32_t xn = reduce_acc(acc);
                 x[j & 7] = xn;
