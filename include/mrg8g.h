@@ -193,6 +193,95 @@ MRG8G_API int mrg8g_batch_set_config(mrg8g_batch *b, const mrg8g_batch_config *c
 MRG8G_API int mrg8g_batch_stats(const mrg8g_batch *b, uint64_t *tiles, uint64_t *outputs, uint64_t *bytes);
 MRG8G_API int mrg8g_batch_destroy(mrg8g_batch *b);
 
+/* ---- serving: continuous batching of draw requests ---------------------- */
+
+/* A server keeps generator states resident on the device and serves draw
+ * requests: a scheduler thread admits them first-in first-out against a
+ * device output arena (the admission budget), packs whatever is admitted into
+ * one batch launch (the batch kernel above) on one of `inflight` streams, and
+ * keeps admitting and launching while earlier batches run, so requests that
+ * arrive while others are on the GPU are admitted as slots and memory free up
+ * and their work overlaps on the device.  Each result equals the request's own
+ * stream segment whatever else is in flight.  No reference counterpart. */
+typedef struct mrg8g_server_config {
+    uint64_t budget_bytes;   /* output arena = admission budget (0: 16 GiB)  */
+    uint32_t max_batch;      /* requests per launch at most (0: 1024)        */
+    uint32_t inflight;       /* launches in flight, one stream each (0: 3)   */
+    uint32_t max_generators; /* device-resident generator slots (0: 65536)   */
+    int32_t tile_rows;       /* batch-kernel tile rows (0: 256)              */
+    int32_t threads;         /* batch-kernel block size, 128 or 256 (0: 128) */
+    int32_t reserved;        /* 0                                            */
+} mrg8g_server_config;
+
+#define MRG8G_NO_GENERATOR 0xFFFFFFFFu
+
+typedef struct mrg8g_request {
+    uint32_t generator; /* slot of a registered generator (its draws continue
+                           its stream), or MRG8G_NO_GENERATOR              */
+    uint32_t seed;      /* without a generator: the stream seeded by `seed` */
+    uint64_t offset;    /* ... starting `offset` outputs in                 */
+    uint64_t n;         /* outputs                                          */
+    int32_t kind;       /* MRG8G_U32 ... MRG8G_F32_SHIFTED                   */
+    int32_t reserved;   /* 0                                                */
+    uint64_t tag;       /* returned with the completion                     */
+} mrg8g_request;
+
+typedef struct mrg8g_completion {
+    uint64_t ticket;
+    uint64_t tag;
+    void *out;          /* device pointer to the n outputs, valid until
+                           mrg8g_server_release(ticket)                     */
+    uint64_t n;
+    int32_t kind;
+    int32_t status;     /* MRG8G_SUCCESS or the error that failed the batch */
+    double t_submit, t_admit, t_done; /* host steady clock, seconds         */
+} mrg8g_completion;
+
+typedef struct mrg8g_server_stats {
+    uint64_t submitted, completed, pending, launches, launched_requests, samples;
+    uint64_t bytes_in_use, peak_bytes;
+    int32_t error, reserved;
+} mrg8g_server_stats;
+
+typedef struct mrg8g_server mrg8g_server;
+
+MRG8G_API int mrg8g_server_create(const mrg8g_server_config *cfg, mrg8g_server **out);
+/* Register a generator (its state goes to the device table); *slot names it. */
+MRG8G_API int mrg8g_server_add_generator(mrg8g_server *s, const uint32_t state[8], uint32_t *slot);
+/* The generator's state after every draw submitted so far. */
+MRG8G_API int mrg8g_server_generator_state(mrg8g_server *s, uint32_t slot, uint32_t state[8]);
+/* Queue a request (thread-safe, returns at once); MRG8G_ERR_BUDGET if it can
+ * never fit the arena. */
+MRG8G_API int mrg8g_server_submit(mrg8g_server *s, const mrg8g_request *req, uint64_t *ticket);
+/* Up to `max` completed requests, waiting at most timeout_us for the first. */
+MRG8G_API int mrg8g_server_poll(mrg8g_server *s, mrg8g_completion *out, uint32_t max, uint32_t *count,
+                                uint32_t timeout_us);
+/* Copy a completed request's outputs to host memory (bytes <= n * element
+ * size; synchronous). */
+MRG8G_API int mrg8g_server_read(mrg8g_server *s, uint64_t ticket, void *host, uint64_t bytes);
+/* Give a completed request's output region back to the arena. */
+MRG8G_API int mrg8g_server_release(mrg8g_server *s, uint64_t ticket);
+MRG8G_API int mrg8g_server_get_stats(mrg8g_server *s, mrg8g_server_stats *st);
+/* Stops the scheduler after the work in flight and frees everything. */
+MRG8G_API int mrg8g_server_destroy(mrg8g_server *s);
+
+/* Open-loop load test: Poisson arrivals at `rate` per second for
+ * `duration_s`; lengths log-uniform in [n_min, n_max]; offsets uniform in
+ * [0, offset_max); kinds uniform over the set bits of kinds_mask (bit k =
+ * kind k); random seeds; each result held hold_us, then released. */
+typedef struct mrg8g_loadtest_config {
+    double rate, duration_s, hold_us;
+    uint64_t n_min, n_max, offset_max, rng_seed;
+    uint32_t kinds_mask, reserved;
+} mrg8g_loadtest_config;
+
+typedef struct mrg8g_loadtest_result {
+    uint64_t requests, samples, bytes, launches, peak_bytes, late_submits;
+    double wall_s, gsamples_per_s, mean_us, p50_us, p90_us, p99_us, max_us, mean_batch;
+} mrg8g_loadtest_result;
+
+MRG8G_API int mrg8g_server_loadtest(mrg8g_server *s, const mrg8g_loadtest_config *cfg, mrg8g_loadtest_result *res);
+
 /* ---- utilities ---------------------------------------------------------- */
 
 /* st = the state seeded from `seed` by mcg64ni (original/mrg8.cpp:180-194). */

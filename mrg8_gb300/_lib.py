@@ -62,6 +62,16 @@ SIGNATURES: dict[str, tuple] = {
     "mrg8g_batch_set_config": (_int, [_vp, _vp]),
     "mrg8g_batch_stats": (_int, [_vp, _vp, _vp, _vp]),
     "mrg8g_batch_destroy": (_int, [_vp]),
+    "mrg8g_server_create": (_int, [_vp, _vp]),
+    "mrg8g_server_add_generator": (_int, [_vp, _vp, _vp]),
+    "mrg8g_server_generator_state": (_int, [_vp, _u32, _vp]),
+    "mrg8g_server_submit": (_int, [_vp, _vp, _vp]),
+    "mrg8g_server_poll": (_int, [_vp, _vp, _u32, _vp, _u32]),
+    "mrg8g_server_read": (_int, [_vp, _u64, _vp, _u64]),
+    "mrg8g_server_release": (_int, [_vp, _u64]),
+    "mrg8g_server_get_stats": (_int, [_vp, _vp]),
+    "mrg8g_server_destroy": (_int, [_vp]),
+    "mrg8g_server_loadtest": (_int, [_vp, _vp, _vp]),
 }
 
 
@@ -69,6 +79,52 @@ class Instance(C.Structure):
     """mrg8g_instance of include/mrg8g.h."""
     _fields_ = [("state", C.c_uint32 * 8), ("offset", C.c_uint64), ("n", C.c_uint64), ("out", C.c_void_p),
                 ("kind", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    """mrg8g_server_config of include/mrg8g.h."""
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_batch", C.c_uint32), ("inflight", C.c_uint32),
+                ("max_generators", C.c_uint32), ("tile_rows", C.c_int32), ("threads", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+NO_GENERATOR = 0xFFFFFFFF
+
+
+class Request(C.Structure):
+    """mrg8g_request of include/mrg8g.h."""
+    _fields_ = [("generator", C.c_uint32), ("seed", C.c_uint32), ("offset", C.c_uint64), ("n", C.c_uint64),
+                ("kind", C.c_int32), ("reserved", C.c_int32), ("tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    """mrg8g_completion of include/mrg8g.h."""
+    _fields_ = [("ticket", C.c_uint64), ("tag", C.c_uint64), ("out", C.c_void_p), ("n", C.c_uint64),
+                ("kind", C.c_int32), ("status", C.c_int32), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    """mrg8g_server_stats of include/mrg8g.h."""
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("pending", C.c_uint64),
+                ("launches", C.c_uint64), ("launched_requests", C.c_uint64), ("samples", C.c_uint64),
+                ("bytes_in_use", C.c_uint64), ("peak_bytes", C.c_uint64), ("error", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class LoadtestConfig(C.Structure):
+    """mrg8g_loadtest_config of include/mrg8g.h."""
+    _fields_ = [("rate", C.c_double), ("duration_s", C.c_double), ("hold_us", C.c_double), ("n_min", C.c_uint64),
+                ("n_max", C.c_uint64), ("offset_max", C.c_uint64), ("rng_seed", C.c_uint64),
+                ("kinds_mask", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class LoadtestResult(C.Structure):
+    """mrg8g_loadtest_result of include/mrg8g.h."""
+    _fields_ = [("requests", C.c_uint64), ("samples", C.c_uint64), ("bytes", C.c_uint64), ("launches", C.c_uint64),
+                ("peak_bytes", C.c_uint64), ("late_submits", C.c_uint64), ("wall_s", C.c_double),
+                ("gsamples_per_s", C.c_double), ("mean_us", C.c_double), ("p50_us", C.c_double),
+                ("p90_us", C.c_double), ("p99_us", C.c_double), ("max_us", C.c_double), ("mean_batch", C.c_double)]
 
 
 class BatchConfig(C.Structure):

@@ -45,9 +45,10 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
         if (ti >= a.ntiles) break;
         const BatchTile t = a.tiles[ti];
         const BatchInst in = a.insts[t.inst];
+        const uint32_t* src = in.slot1 ? a.states + 8ull * (in.slot1 - 1) : in.st;
         uint32_t s[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s[q] = in.st[q];
+        for (int q = 0; q < 8; ++q) s[q] = src[q];
         warp_jump(g_jump, s, in.offset + t.start);
         if (t.len_flags & kTileHead) {
             if (lane == 0) {

@@ -15,6 +15,33 @@
 
 using namespace mrg8g;
 
+namespace mrg8g {
+
+// Tiles of every instance: an unaligned head (fewer outputs than one 16-byte
+// vector) and body tiles of tile_rows rows; ordered by bytes, largest first,
+// so the dynamic queue ends with the smallest pieces.
+void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vector<BatchTile>& tiles) {
+    tiles.clear();
+    for (uint32_t i = 0; i < count; ++i) {
+        const BatchInst& in = insts[i];
+        if (in.n == 0) continue;
+        const int elem = kind_elem_bytes(in.kind);
+        const uint64_t V = (uint64_t)default_layout_V(in.kind);
+        const uint64_t T = (uint64_t)tile_rows * 32 * V;
+        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
+        if (head > in.n) head = in.n;
+        if (head) tiles.push_back({0, i, (uint32_t)head | kTileHead});
+        for (uint64_t s = head; s < in.n; s += T) tiles.push_back({s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)});
+    }
+    std::stable_sort(tiles.begin(), tiles.end(), [&](const BatchTile& x, const BatchTile& y) {
+        const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(insts[x.inst].kind);
+        const uint64_t by = (uint64_t)(y.len_flags & ~kTileHead) * kind_elem_bytes(insts[y.inst].kind);
+        return bx > by;
+    });
+}
+
+}  // namespace mrg8g
+
 struct mrg8g_batch {
     int dev = -1;
     std::vector<BatchInst> insts;
@@ -50,28 +77,8 @@ int normalise(mrg8g_batch_config& c) {
     return MRG8G_SUCCESS;
 }
 
-// Tiles of every instance: an unaligned head (fewer outputs than one 16-byte
-// vector) and body tiles of tile_rows rows; ordered by bytes, largest first,
-// so the dynamic queue ends with the smallest pieces.
 void build_tiles(mrg8g_batch* b) {
-    b->tiles.clear();
-    for (uint32_t i = 0; i < (uint32_t)b->insts.size(); ++i) {
-        const BatchInst& in = b->insts[i];
-        if (in.n == 0) continue;
-        const int elem = kind_elem_bytes(in.kind);
-        const uint64_t V = (uint64_t)default_layout_V(in.kind);
-        const uint64_t T = (uint64_t)b->cfg.tile_rows * 32 * V;
-        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
-        if (head > in.n) head = in.n;
-        if (head) b->tiles.push_back({0, i, (uint32_t)head | kTileHead});
-        for (uint64_t s = head; s < in.n; s += T)
-            b->tiles.push_back({s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)});
-    }
-    std::stable_sort(b->tiles.begin(), b->tiles.end(), [&](const BatchTile& x, const BatchTile& y) {
-        const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(b->insts[x.inst].kind);
-        const uint64_t by = (uint64_t)(y.len_flags & ~kTileHead) * kind_elem_bytes(b->insts[y.inst].kind);
-        return bx > by;
-    });
+    make_tiles(b->insts.data(), (uint32_t)b->insts.size(), b->cfg.tile_rows, b->tiles);
 }
 
 int upload_tiles(mrg8g_batch* b) {
@@ -117,6 +124,7 @@ BatchArgs args_of(const mrg8g_batch* b) {
     a.tiles = b->d_tiles;
     a.ntiles = (uint32_t)b->tiles.size();
     a.counter = b->d_counter;
+    a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     return a;
 }
@@ -202,7 +210,7 @@ int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_b
         d.n = s.n;
         d.out = s.out;
         d.kind = s.kind;
-        d.pad = 0;
+        d.slot1 = 0;
         b->outputs += s.n;
         b->bytes += s.n * elem;
     }

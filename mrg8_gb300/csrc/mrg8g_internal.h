@@ -28,14 +28,16 @@ struct JumpArgs {
 
 // ---- batches of independent instances
 
-// Device copy of one instance (mrg8g_instance of the C ABI).
+// Device copy of one instance (mrg8g_instance of the C ABI).  slot1 = 0: the
+// state is st; slot1 = k + 1: the state is row k of the device-resident
+// generator table (serving), st unused.
 struct BatchInst {
     uint32_t st[8];
     uint64_t offset;
     uint64_t n;
     void* out;
     int32_t kind;
-    int32_t pad;
+    uint32_t slot1;
 };
 
 // One unit of work: outputs [start, start + len) of instance `inst`.  Bit 31
@@ -52,7 +54,8 @@ struct BatchArgs {
     const BatchInst* insts;
     const BatchTile* tiles;
     uint32_t ntiles;
-    uint32_t* counter;  // work-queue position, zero before each launch
+    uint32_t* counter;        // work-queue position, zero before each launch
+    const uint32_t* states;   // generator table (8 words per slot) or null
     LeapCoef leap[kNumLayouts];
 };
 

@@ -5,6 +5,9 @@
 #include <stdint.h>
 
 #include <cstdarg>
+#include <vector>
+
+#include "mrg8g_internal.h"
 
 namespace mrg8g {
 
@@ -26,5 +29,8 @@ void advance_state(uint32_t st[8], uint64_t n);
 int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, cudaStream_t s, int V);
 
 cudaError_t upload_tables_batch();
+
+// Tiles of a batch (see mrg8g_batch_host.cpp).
+void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vector<BatchTile>& tiles);
 
 }  // namespace mrg8g

@@ -1,0 +1,616 @@
+// mrg8g_serve.cpp -- serving: continuous batching of draw requests.
+//
+// A scheduler thread admits requests first-in first-out against a device
+// output arena (the admission budget), packs the admitted ones into a batch
+// (the tiles of the batch kernel, mrg8g_batch.cu) and launches it on one of
+// several streams, so that requests arriving while others are on the GPU are
+// admitted as soon as a stream slot and arena space are free and their work
+// overlaps on the device.  Generator states live in a device table; a draw
+// from a registered generator continues its stream (the host keeps only the
+// position).  Completion times are taken by a host callback enqueued after
+// each batch.  Nothing on the device waits: the kernels are the batch kernel
+// and the scheduler waits on the host with bounded timeouts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <string>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/mrg8g.h"
+#include "mrg8g_internal.h"
+#include "mrg8g_runtime.h"
+#include "mrg8g_tables.h"
+
+using namespace mrg8g;
+
+namespace {
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// First-in first-out arena over [0, cap): blocks are handed out in admission
+// order and reclaimed from the oldest once released (out-of-order releases
+// wait for the older ones).  256-byte granularity.
+class Arena {
+public:
+    explicit Arena(uint64_t cap) : cap_(cap) {}
+    bool alloc(uint64_t bytes, uint64_t* off) {
+        bytes = bytes ? (bytes + 255) / 256 * 256 : 256;
+        if (bytes > cap_) return false;
+        if (blocks_.empty()) head_ = tail_ = 0;
+        // Live blocks occupy [tail, head) or, once wrapped, [tail, cap) + [0, head).
+        const bool wrapped = !blocks_.empty() && head_ <= tail_;
+        uint64_t at;
+        if (!wrapped) {
+            if (cap_ - head_ >= bytes) {
+                at = head_;
+            } else if (tail_ >= bytes) {
+                if (head_ < cap_) blocks_.push_back({head_, cap_ - head_, true});  // unused end
+                at = 0;
+            } else {
+                return false;
+            }
+        } else if (tail_ - head_ >= bytes) {
+            at = head_;
+        } else {
+            return false;
+        }
+        blocks_.push_back({at, bytes, false});
+        head_ = at + bytes;
+        used_ += bytes;
+        *off = at;
+        return true;
+    }
+    void release(uint64_t off) {
+        for (auto& b : blocks_)
+            if (b.off == off && !b.released) {
+                b.released = true;
+                used_ -= b.size;
+                break;
+            }
+        while (!blocks_.empty() && blocks_.front().released) blocks_.pop_front();
+        if (blocks_.empty()) head_ = tail_ = 0;
+        else tail_ = blocks_.front().off;
+    }
+    uint64_t used() const { return used_; }
+
+private:
+    struct Block {
+        uint64_t off, size;
+        bool released;
+    };
+    uint64_t cap_, head_ = 0, tail_ = 0, used_ = 0;
+    std::deque<Block> blocks_;
+};
+
+struct Req {
+    mrg8g_request r;
+    uint32_t state[8];  // stateless requests
+    uint64_t offset;    // jump distance from the (embedded or table) state
+    uint64_t bytes = 0, arena_off = 0;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int status = MRG8G_SUCCESS;
+    bool done = false;
+};
+
+struct Slot {
+    int idx = 0;
+    cudaStream_t stream = nullptr;
+    BatchInst* d_insts = nullptr;
+    BatchTile* d_tiles = nullptr;
+    uint32_t* d_counter = nullptr;
+    BatchInst* h_insts = nullptr;  // pinned staging
+    BatchTile* h_tiles = nullptr;
+    size_t tiles_cap = 0;
+    std::vector<uint64_t> tickets;
+    bool busy = false;
+    mrg8g_server* server = nullptr;
+};
+
+}  // namespace
+
+struct mrg8g_server {
+    mrg8g_server_config cfg{};
+    int dev = 0, sms = 0, bps = 1;
+    void* arena_base = nullptr;
+    uint32_t* d_states = nullptr;
+    std::vector<uint64_t> gen_pos;
+    std::vector<std::array<uint32_t, 8>> gen_state;
+    std::unique_ptr<Arena> arena;
+    std::vector<Slot> slots;
+
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::deque<uint64_t> pending;  // admission order
+    std::deque<uint64_t> completed;
+    std::deque<int> done_slots;
+    std::vector<double> done_times;
+    std::unordered_map<uint64_t, Req> reqs;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+    int error = MRG8G_SUCCESS;
+    std::string error_msg;
+    std::thread thread;
+
+    // statistics
+    uint64_t submitted = 0, finished = 0, launches = 0, launched_requests = 0, samples = 0, peak_bytes = 0;
+};
+
+namespace {
+
+void CUDART_CB on_slot_done(void* p) {
+    Slot* s = static_cast<Slot*>(p);
+    mrg8g_server* sv = s->server;
+    const double t = now_s();
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->done_times[s->idx] = t;
+    sv->done_slots.push_back(s->idx);
+    sv->cv_sched.notify_one();
+}
+
+// Descriptors of the tickets admitted to slot `sl` (lock held).
+void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, std::vector<BatchTile>& tiles) {
+    const uint32_t count = (uint32_t)sl.tickets.size();
+    insts.resize(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const Req& q = sv->reqs[sl.tickets[i]];
+        BatchInst& d = insts[i];
+        std::memcpy(d.st, q.state, sizeof(d.st));
+        d.offset = q.offset;
+        d.n = q.r.n;
+        d.out = static_cast<char*>(sv->arena_base) + q.arena_off;
+        d.kind = q.r.kind;
+        d.slot1 = q.r.generator == MRG8G_NO_GENERATOR ? 0u : q.r.generator + 1u;
+    }
+    make_tiles(insts.data(), count, sv->cfg.tile_rows, tiles);
+}
+
+// Enqueue slot `sl`'s batch on its stream (lock not held; the slot is owned
+// by the scheduler thread while busy).
+int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts, const std::vector<BatchTile>& tiles) {
+    const size_t count = insts.size();
+    if (tiles.size() > sl.tiles_cap) return fail(MRG8G_ERR_BUDGET, "batch needs %zu tiles (cap %zu)", tiles.size(), sl.tiles_cap);
+    std::memcpy(sl.h_insts, insts.data(), count * sizeof(BatchInst));
+    std::memcpy(sl.h_tiles, tiles.data(), tiles.size() * sizeof(BatchTile));
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(sl.d_insts, sl.h_insts, count * sizeof(BatchInst), cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "serving: copy of instances");
+    if (!tiles.empty() &&
+        (e = cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
+                             sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "serving: copy of tiles");
+    if ((e = cudaMemsetAsync(sl.d_counter, 0, sizeof(uint32_t), sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "serving: counter reset");
+    if (!tiles.empty()) {
+        BatchArgs a;
+        a.insts = sl.d_insts;
+        a.tiles = sl.d_tiles;
+        a.ntiles = (uint32_t)tiles.size();
+        a.counter = sl.d_counter;
+        a.states = sv->d_states;
+        for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+        const uint64_t wpb = (uint64_t)sv->cfg.threads / 32;
+        const uint64_t want = (tiles.size() + wpb - 1) / wpb;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sv->sms * sv->bps, want));
+        if ((e = launch_batch(a, sv->cfg.threads, blocks, sl.stream)) != cudaSuccess)
+            return cuda_fail(e, "serving: batch launch");
+    }
+    if ((e = cudaLaunchHostFunc(sl.stream, on_slot_done, &sl)) != cudaSuccess)
+        return cuda_fail(e, "serving: completion callback");
+    return MRG8G_SUCCESS;
+}
+
+void scheduler(mrg8g_server* sv) {
+    cudaSetDevice(sv->dev);
+    std::vector<BatchInst> insts;
+    std::vector<BatchTile> tiles;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    while (!sv->stop) {
+        // Finished launches: their requests complete with the callback time.
+        bool any_done = false;
+        while (!sv->done_slots.empty()) {
+            Slot& sl = sv->slots[sv->done_slots.front()];
+            sv->done_slots.pop_front();
+            const double t = sv->done_times[sl.idx];
+            for (uint64_t tk : sl.tickets) {
+                Req& q = sv->reqs[tk];
+                q.t_done = t;
+                q.done = true;
+                sv->completed.push_back(tk);
+                sv->finished++;
+                sv->samples += q.r.n;
+            }
+            sl.tickets.clear();
+            sl.busy = false;
+            any_done = true;
+        }
+        if (any_done) sv->cv_done.notify_all();
+        // Admission into free slots, first in first out.
+        for (Slot& sl : sv->slots) {
+            if (sl.busy || sv->pending.empty() || sv->error) continue;
+            const double t = now_s();
+            while (!sv->pending.empty() && sl.tickets.size() < sv->cfg.max_batch) {
+                Req& q = sv->reqs[sv->pending.front()];
+                if (!sv->arena->alloc(q.bytes, &q.arena_off)) break;  // head of line waits for space
+                q.t_admit = t;
+                sl.tickets.push_back(sv->pending.front());
+                sv->pending.pop_front();
+            }
+            if (sl.tickets.empty()) break;
+            sv->peak_bytes = std::max(sv->peak_bytes, sv->arena->used());
+            describe_slot(sv, sl, insts, tiles);
+            sl.busy = true;
+            sv->launches++;
+            sv->launched_requests += sl.tickets.size();
+            lk.unlock();
+            const int rc = enqueue_slot(sv, sl, insts, tiles);
+            std::string msg = rc ? mrg8g_last_error() : "";
+            lk.lock();
+            if (rc) {
+                sv->error = rc;
+                sv->error_msg = msg;
+                for (uint64_t tk : sl.tickets) {
+                    Req& q = sv->reqs[tk];
+                    q.status = rc;
+                    q.done = true;
+                    q.t_done = now_s();
+                    sv->completed.push_back(tk);
+                }
+                sl.tickets.clear();
+                sl.busy = false;
+                sv->cv_done.notify_all();
+            }
+        }
+        sv->cv_sched.wait_for(lk, std::chrono::microseconds(500));
+    }
+}
+
+void destroy_server(mrg8g_server* sv) {
+    if (sv->thread.joinable()) {
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->stop = true;
+            sv->cv_sched.notify_all();
+        }
+        sv->thread.join();
+    }
+    for (Slot& sl : sv->slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream), cudaStreamDestroy(sl.stream);
+        if (sl.d_insts) cudaFree(sl.d_insts);
+        if (sl.d_tiles) cudaFree(sl.d_tiles);
+        if (sl.d_counter) cudaFree(sl.d_counter);
+        if (sl.h_insts) cudaFreeHost(sl.h_insts);
+        if (sl.h_tiles) cudaFreeHost(sl.h_tiles);
+    }
+    if (sv->arena_base) cudaFree(sv->arena_base);
+    if (sv->d_states) cudaFree(sv->d_states);
+    delete sv;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
+    if (!out) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    mrg8g_server_config c{};
+    if (cfg) c = *cfg;
+    if (!c.budget_bytes) c.budget_bytes = 16ull << 30;
+    if (!c.max_batch) c.max_batch = 1024;
+    if (!c.inflight) c.inflight = 3;
+    if (!c.max_generators) c.max_generators = 65536;
+    if (!c.tile_rows) c.tile_rows = 256;
+    if (!c.threads) c.threads = 128;
+    if (c.tile_rows < 8 || (c.tile_rows & 7) || c.tile_rows > (1 << 16) || (c.threads != 128 && c.threads != 256) ||
+        c.inflight > 16)
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "bad server configuration");
+    int dev = 0;
+    int rc = ensure_device(&dev, nullptr);
+    if (rc) return rc;
+    mrg8g_server* sv = new (std::nothrow) mrg8g_server;
+    if (!sv) return fail(MRG8G_ERR_OUT_OF_MEMORY, "host allocation failed");
+    sv->cfg = c;
+    sv->dev = dev;
+    sv->sms = device_sms();
+    sv->bps = batch_blocks_per_sm(c.threads);
+    sv->arena.reset(new Arena(c.budget_bytes));
+    sv->gen_pos.reserve(1024);
+    cudaError_t e;
+    if ((e = cudaMalloc(&sv->arena_base, c.budget_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&sv->d_states, (size_t)c.max_generators * 8 * sizeof(uint32_t))) != cudaSuccess) {
+        destroy_server(sv);
+        return cuda_fail(e, "serving: arena allocation");
+    }
+    // Tiles per launch are bounded by the arena (every tile but a head covers
+    // at least one row, and a full tile covers tile_rows * 512 bytes).
+    const size_t min_tile_bytes = (size_t)c.tile_rows * 32 * 4 * 4;
+    const size_t tiles_cap = c.budget_bytes / min_tile_bytes + 3 * (size_t)c.max_batch + 16;
+    sv->slots.resize(c.inflight);
+    sv->done_times.assign(c.inflight, 0.0);
+    for (uint32_t i = 0; i < c.inflight; ++i) {
+        Slot& sl = sv->slots[i];
+        sl.idx = (int)i;
+        sl.server = sv;
+        sl.tiles_cap = tiles_cap;
+        if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaMalloc(&sl.d_insts, c.max_batch * sizeof(BatchInst))) != cudaSuccess ||
+            (e = cudaMalloc(&sl.d_tiles, tiles_cap * sizeof(BatchTile))) != cudaSuccess ||
+            (e = cudaMalloc(&sl.d_counter, sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaHostAlloc(&sl.h_insts, c.max_batch * sizeof(BatchInst), cudaHostAllocDefault)) != cudaSuccess ||
+            (e = cudaHostAlloc(&sl.h_tiles, tiles_cap * sizeof(BatchTile), cudaHostAllocDefault)) != cudaSuccess) {
+            destroy_server(sv);
+            return cuda_fail(e, "serving: slot allocation");
+        }
+    }
+    try {
+        sv->thread = std::thread(scheduler, sv);
+    } catch (...) {
+        destroy_server(sv);
+        return fail(MRG8G_ERR_OUT_OF_MEMORY, "cannot start the scheduler thread");
+    }
+    *out = sv;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_add_generator(mrg8g_server* sv, const uint32_t state[8], uint32_t* slot) {
+    if (!sv || !state || !slot) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    int rc = validate_state(state);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->gen_pos.size() >= sv->cfg.max_generators) return fail(MRG8G_ERR_BUDGET, "generator table is full");
+    const uint32_t k = (uint32_t)sv->gen_pos.size();
+    cudaError_t e = cudaMemcpy(sv->d_states + 8ull * k, state, 8 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "serving: generator upload");
+    std::array<uint32_t, 8> st;
+    std::memcpy(st.data(), state, sizeof(uint32_t) * 8);
+    sv->gen_state.push_back(st);
+    sv->gen_pos.push_back(0);
+    *slot = k;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_generator_state(mrg8g_server* sv, uint32_t slot, uint32_t state[8]) {
+    if (!sv || !state) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    uint32_t base[8];
+    uint64_t pos;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (slot >= sv->gen_pos.size()) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown generator %u", slot);
+        std::memcpy(base, sv->gen_state[slot].data(), sizeof(base));
+        pos = sv->gen_pos[slot];
+    }
+    std::memcpy(state, base, sizeof(base));
+    advance_state(state, pos);
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_submit(mrg8g_server* sv, const mrg8g_request* r, uint64_t* ticket) {
+    if (!sv || !r || !ticket) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    if (!kind_valid(r->kind)) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown kind %d", r->kind);
+    const uint64_t bytes = r->n * (uint64_t)kind_elem_bytes(r->kind);
+    if (r->n > (1ull << 40) || bytes > sv->cfg.budget_bytes)
+        return fail(MRG8G_ERR_BUDGET, "request of %llu bytes exceeds the budget", (unsigned long long)bytes);
+    Req q;
+    q.r = *r;
+    q.bytes = bytes;
+    q.t_submit = now_s();
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (sv->error) return fail(sv->error, "server failed: %s", sv->error_msg.c_str());
+    if (r->generator == MRG8G_NO_GENERATOR) {
+        mcg64ni(r->seed, q.state);
+        q.offset = r->offset;
+        if (r->offset > ~0ull - r->n) return fail(MRG8G_ERR_INVALID_ARGUMENT, "offset + n overflows");
+    } else {
+        if (r->generator >= sv->gen_pos.size()) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown generator");
+        std::memset(q.state, 0, sizeof(q.state));
+        q.offset = sv->gen_pos[r->generator];
+        sv->gen_pos[r->generator] += r->n;
+    }
+    const uint64_t tk = sv->next_ticket++;
+    sv->reqs.emplace(tk, q);
+    sv->pending.push_back(tk);
+    sv->submitted++;
+    sv->cv_sched.notify_one();
+    *ticket = tk;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_poll(mrg8g_server* sv, mrg8g_completion* out, uint32_t max, uint32_t* count, uint32_t timeout_us) {
+    if (!sv || !count || (max && !out)) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (sv->completed.empty() && timeout_us)
+        sv->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), [&] { return !sv->completed.empty(); });
+    uint32_t k = 0;
+    while (k < max && !sv->completed.empty()) {
+        const uint64_t tk = sv->completed.front();
+        sv->completed.pop_front();
+        const Req& q = sv->reqs[tk];
+        mrg8g_completion& c = out[k++];
+        c.ticket = tk;
+        c.tag = q.r.tag;
+        c.out = static_cast<char*>(sv->arena_base) + q.arena_off;
+        c.n = q.r.n;
+        c.kind = q.r.kind;
+        c.status = q.status;
+        c.t_submit = q.t_submit;
+        c.t_admit = q.t_admit;
+        c.t_done = q.t_done;
+    }
+    *count = k;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_read(mrg8g_server* sv, uint64_t ticket, void* host, uint64_t bytes) {
+    if (!sv || (bytes && !host)) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    const void* src = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        auto it = sv->reqs.find(ticket);
+        if (it == sv->reqs.end()) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
+        const Req& q = it->second;
+        if (!q.done) return fail(MRG8G_ERR_NOT_READY, "ticket %llu is not complete", (unsigned long long)ticket);
+        if (q.status) return fail(q.status, "ticket %llu failed", (unsigned long long)ticket);
+        if (bytes > q.bytes) return fail(MRG8G_ERR_INVALID_ARGUMENT, "read past the result");
+        src = static_cast<const char*>(sv->arena_base) + q.arena_off;
+    }
+    cudaError_t e = cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "serving: result read");
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_release(mrg8g_server* sv, uint64_t ticket) {
+    if (!sv) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null server");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end()) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
+    if (!it->second.done) return fail(MRG8G_ERR_NOT_READY, "ticket %llu is not complete", (unsigned long long)ticket);
+    if (it->second.t_admit > 0) sv->arena->release(it->second.arena_off);
+    sv->reqs.erase(it);
+    sv->cv_sched.notify_one();
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_get_stats(mrg8g_server* sv, mrg8g_server_stats* st) {
+    if (!sv || !st) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    st->submitted = sv->submitted;
+    st->completed = sv->finished;
+    st->pending = sv->pending.size();
+    st->launches = sv->launches;
+    st->launched_requests = sv->launched_requests;
+    st->samples = sv->samples;
+    st->bytes_in_use = sv->arena->used();
+    st->peak_bytes = sv->peak_bytes;
+    st->error = sv->error;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_server_destroy(mrg8g_server* sv) {
+    if (!sv) return MRG8G_SUCCESS;
+    destroy_server(sv);
+    return MRG8G_SUCCESS;
+}
+
+// Open-loop Poisson load: arrivals at `rate` per second for `duration_s`,
+// lengths log-uniform in [n_min, n_max], offsets uniform in [0, offset_max),
+// kinds uniform over kinds_mask, seeds random; every completion is held for
+// hold_us and then released.  Latency = completion time - submit time.
+int mrg8g_server_loadtest(mrg8g_server* sv, const mrg8g_loadtest_config* cfg, mrg8g_loadtest_result* res) {
+    if (!sv || !cfg || !res) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    if (cfg->rate <= 0 || cfg->duration_s <= 0 || cfg->n_min == 0 || cfg->n_max < cfg->n_min || !(cfg->kinds_mask & 31))
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "bad load-test configuration");
+    std::mt19937_64 rng(cfg->rng_seed);
+    std::exponential_distribution<double> gap(cfg->rate);
+    std::uniform_real_distribution<double> u01(0.0, 1.0);
+    std::vector<int> kinds;
+    for (int k = 0; k < 5; ++k)
+        if (cfg->kinds_mask & (1u << k)) kinds.push_back(k);
+    std::atomic<bool> done_submitting{false};
+    std::atomic<uint64_t> submitted{0};
+    std::vector<double> lat;
+    lat.reserve((size_t)(cfg->rate * cfg->duration_s * 1.2) + 16);
+    uint64_t samples = 0, bytes = 0;
+    double t_first = 0, t_last = 0;
+    int consumer_rc = MRG8G_SUCCESS;
+    std::thread consumer([&] {
+        std::vector<mrg8g_completion> buf(256);
+        std::deque<std::pair<double, uint64_t>> held;
+        uint64_t seen = 0;
+        while (true) {
+            uint32_t n = 0;
+            int rc = mrg8g_server_poll(sv, buf.data(), (uint32_t)buf.size(), &n, 200);
+            if (rc) {
+                consumer_rc = rc;
+                break;
+            }
+            const double t = now_s();
+            for (uint32_t i = 0; i < n; ++i) {
+                const mrg8g_completion& c = buf[i];
+                if (c.status) consumer_rc = c.status;
+                lat.push_back(c.t_done - c.t_submit);
+                samples += c.n;
+                bytes += c.n * kind_elem_bytes(c.kind);
+                t_last = std::max(t_last, c.t_done);
+                held.push_back({t + cfg->hold_us * 1e-6, c.ticket});
+            }
+            seen += n;
+            while (!held.empty() && held.front().first <= now_s()) {
+                mrg8g_server_release(sv, held.front().second);
+                held.pop_front();
+            }
+            if (done_submitting.load() && seen >= submitted.load()) {
+                for (auto& h : held) mrg8g_server_release(sv, h.second);
+                break;
+            }
+        }
+    });
+    const double t0 = now_s();
+    t_first = t0;
+    double t_next = t0;
+    uint64_t late = 0, count = 0;
+    const double lmin = std::log((double)cfg->n_min), lmax = std::log((double)cfg->n_max + 1.0);
+    int rc = MRG8G_SUCCESS;
+    while (true) {
+        t_next += gap(rng);
+        if (t_next - t0 > cfg->duration_s) break;
+        mrg8g_request r{};
+        r.generator = MRG8G_NO_GENERATOR;
+        r.seed = (uint32_t)rng();
+        r.offset = cfg->offset_max ? rng() % cfg->offset_max : 0;
+        r.n = std::min<uint64_t>(cfg->n_max, (uint64_t)std::exp(lmin + (lmax - lmin) * u01(rng)));
+        r.kind = kinds[rng() % kinds.size()];
+        r.tag = count;
+        double t;
+        while ((t = now_s()) < t_next) {
+        }
+        if (t - t_next > 100e-6) late++;
+        uint64_t tk;
+        rc = mrg8g_server_submit(sv, &r, &tk);
+        if (rc) break;
+        submitted.fetch_add(1);
+        count++;
+    }
+    done_submitting.store(true);
+    consumer.join();
+    if (rc) return rc;
+    if (consumer_rc) return consumer_rc;
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double p) { return lat.empty() ? 0.0 : lat[std::min(lat.size() - 1, (size_t)(p * (lat.size() - 1) + 0.5))]; };
+    mrg8g_server_stats st;
+    mrg8g_server_get_stats(sv, &st);
+    res->requests = lat.size();
+    res->samples = samples;
+    res->bytes = bytes;
+    res->wall_s = t_last - t_first;
+    res->gsamples_per_s = res->wall_s > 0 ? samples / res->wall_s / 1e9 : 0;
+    double sum = 0;
+    for (double v : lat) sum += v;
+    res->mean_us = lat.empty() ? 0 : sum / lat.size() * 1e6;
+    res->p50_us = pct(0.50) * 1e6;
+    res->p90_us = pct(0.90) * 1e6;
+    res->p99_us = pct(0.99) * 1e6;
+    res->max_us = lat.empty() ? 0 : lat.back() * 1e6;
+    res->launches = st.launches;
+    res->mean_batch = st.launches ? (double)st.launched_requests / st.launches : 0;
+    res->peak_bytes = st.peak_bytes;
+    res->late_submits = late;
+    return MRG8G_SUCCESS;
+}
+
+}  // extern "C"
