@@ -140,6 +140,76 @@ def cpu_baseline(n: int, kind: int, min_seconds: float = 3.0):
     return gs, cores, f"{runs} runs of {n} fp64 SHIFTED samples ({n * 8 >> 20} MiB), first run discarded"
 
 
+def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, seed: int = 4):
+    """Config 4: `count` generators with distinct seeds, lengths log-uniform in
+    [1, 2^max_log2], kinds uniform over fp64/fp32/uint32 (SHIFTED uniforms);
+    one autotuned graph-captured batch launch vs one bulk launch per instance.
+    Both produce the same values (tests/test_batch_gpu.py)."""
+    import numpy as np
+    import torch
+
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(seed)
+    kinds = [m.F64_SHIFTED, m.F32_SHIFTED, m.U32]
+    lens = np.minimum((2.0 ** rng.uniform(0, max_log2, count)).astype(np.int64), 1 << max_log2)
+    ks = rng.integers(0, 3, count)
+    dts = {m.F64_SHIFTED: torch.float64, m.F32_SHIFTED: torch.float32, m.U32: torch.int32}
+    insts = []
+    total = 0
+    nbytes = 0
+    for i in range(count):
+        kind = kinds[int(ks[i])]
+        n = int(lens[i])
+        out = torch.empty(n, dtype=dts[kind], device=dev)
+        insts.append((m.seed_state((i * 2654435761 + 12345) & 0xFFFFFFFF), 0, out, kind))
+        total += n
+        nbytes += n * out.element_size()
+    b = m.Batch(insts)
+    tuned = b.autotune()
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps, (time.perf_counter() - t0) / reps
+
+    tb, wb = timed(b.launch, steps)
+    te, we = timed(b.launch_each, max(2, steps // 2))
+    st = b.stats()
+    b.close()
+    del insts
+    torch.cuda.empty_cache()
+    return {"instances": count, "outputs": total, "bytes": nbytes, "tiles": st["tiles"], "config": tuned,
+            "batched_gsamples_per_s": round(total / tb / 1e9, 3), "batched_ms": round(tb * 1e3, 3),
+            "per_instance_gsamples_per_s": round(total / te / 1e9, 3), "per_instance_ms": round(te * 1e3, 3),
+            "per_instance_wall_ms": round(we * 1e3, 3), "speedup": round(te / tb, 2),
+            "lengths": f"log-uniform in [1, 2^{max_log2}]", "kinds": "fp64/fp32/u32 uniform (SHIFTED)"}
+
+
+def run_served(seconds: float, rate: float = 20_000.0):
+    """Config 5: Poisson arrivals at `rate`/s for `seconds`, offsets uniform in
+    [0, 2^48), lengths log-uniform in [2^8, 2^26], kinds fp64/fp32/uint32,
+    16 GiB admission budget, results released on completion."""
+    from mrg8_gb300.serve import Server
+    with Server(budget_bytes=16 << 30) as srv:
+        srv.loadtest(rate=rate, duration_s=min(1.0, seconds), n_min=1 << 8, n_max=1 << 26, offset_max=1 << 48,
+                     kinds_mask=0b10101, rng_seed=7)  # warm-up
+        r = srv.loadtest(rate=rate, duration_s=seconds, n_min=1 << 8, n_max=1 << 26, offset_max=1 << 48,
+                         kinds_mask=0b10101, rng_seed=11)
+    return {"rate_per_s": rate, "duration_s": seconds, "requests": r["requests"],
+            "gsamples_per_s": round(r["gsamples_per_s"], 3), "p50_us": round(r["p50_us"], 1),
+            "p90_us": round(r["p90_us"], 1), "p99_us": round(r["p99_us"], 1), "max_us": round(r["max_us"], 1),
+            "mean_batch": round(r["mean_batch"], 2), "launches": r["launches"],
+            "peak_bytes": r["peak_bytes"], "late_submits": r["late_submits"], "budget_bytes": 16 << 30}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -290,6 +360,9 @@ def run_gpu(args) -> None:
                        "kernel argument"}
         del host
 
+    batched = None if args.skip_batch or rank else run_batched(dev)
+    served = None if args.skip_serve or rank else run_served(args.serve_seconds)
+
     # Spot check of this run's output against the oracle (first 2^20 values).
     from oracle.pyoracle import F64_SHIFTED as O_F64S, Oracle
     chk = min(n, 1 << 20)
@@ -315,7 +388,8 @@ def run_gpu(args) -> None:
                      "frac": round(achieved / hbm, 4), "peak_source": f"{peak_src} hbm_gbs (copy)",
                      "traffic": traffic, "algorithmic_bytes_per_launch": 8 * n},
         "f32": f32,
-        "e2e": e2e, "cpu_baseline": cpu, "clocks": clk.summary(), "gpu_launches": args.steps,
+        "e2e": e2e, "cpu_baseline": cpu, "batched": batched, "served": served,
+        "clocks": clk.summary(), "gpu_launches": args.steps,
         "parity_spot_check": ok, "wall_s": round(wall, 4),
     }
     print(json.dumps(line), flush=True)
@@ -332,6 +406,9 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-f32", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--n", type=int, default=N_PER_RANK, help="outputs per GPU (profiling of small cases)")
     args = ap.parse_args()
     if args.impl == "reference":

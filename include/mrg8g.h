@@ -184,6 +184,11 @@ MRG8G_API int mrg8g_batch_create(const mrg8g_instance *inst, uint64_t count, con
  * Launches of one plan must not overlap each other on the device. */
 MRG8G_API int mrg8g_batch_launch(mrg8g_batch *b, void *stream);
 
+/* The per-instance path the batch replaces: one bulk-kernel launch per
+ * instance (as one mrg8_cuda::mrg8_outer_32 call per object,
+ * cuda/mrg8_cuda.cu:414-436), all on `stream`.  Same values as a batch. */
+MRG8G_API int mrg8g_generate_each(const mrg8g_instance *inst, uint64_t count, void *stream);
+
 /* Time the candidate shapes on this batch (synchronises `stream`), keep the
  * fastest and report it in *chosen (may be NULL). */
 MRG8G_API int mrg8g_batch_autotune(mrg8g_batch *b, void *stream, mrg8g_batch_config *chosen);

@@ -310,12 +310,19 @@ class Batch:
             items.append(inst)
             self._keep.append(out)
         arr = (_lib.Instance * max(len(items), 1))(*items)
+        self._arr, self._count = arr, len(items)
         cfg = _lib.BatchConfig(tile_rows, threads, blocks_per_sm, 1 if use_graph else 0)
         self.device = device
         h = C.c_void_p()
         with torch.cuda.device(device or torch.cuda.current_device()):
             check(self._lib.mrg8g_batch_create(arr, C.c_uint64(len(items)), C.byref(cfg), C.byref(h)))
         self._h = h
+
+    def launch_each(self, stream=None) -> None:
+        """The per-instance path: one bulk-kernel launch per instance."""
+        with torch.cuda.device(self.device or torch.cuda.current_device()):
+            s = (stream or torch.cuda.current_stream()).cuda_stream
+            check(self._lib.mrg8g_generate_each(self._arr, C.c_uint64(self._count), C.c_void_p(s)))
 
     def launch(self, stream=None) -> None:
         """Enqueue the whole batch (one graph launch) on torch's current

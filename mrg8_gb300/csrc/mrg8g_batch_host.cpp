@@ -310,6 +310,15 @@ int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chose
     return MRG8G_SUCCESS;
 }
 
+int mrg8g_generate_each(const mrg8g_instance* inst, uint64_t count, void* stream) {
+    if (count && !inst) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null instance array");
+    for (uint64_t i = 0; i < count; ++i) {
+        int rc = mrg8g_generate_from_state(inst[i].state, inst[i].offset, inst[i].out, inst[i].n, inst[i].kind, stream);
+        if (rc) return rc;
+    }
+    return MRG8G_SUCCESS;
+}
+
 int mrg8g_batch_destroy(mrg8g_batch* b) {
     if (!b) return MRG8G_SUCCESS;
     destroy_plan(b);

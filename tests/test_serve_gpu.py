@@ -143,3 +143,26 @@ def test_loadtest_smoke(cuda):
     assert r["requests"] > 500
     assert 0 < r["p50_us"] <= r["p99_us"] <= r["max_us"]
     assert r["gsamples_per_s"] > 0
+
+
+def test_request_errors_are_reported(cuda):
+    from mrg8_gb300 import MRG8GError
+    from mrg8_gb300.serve import Server
+    with Server(budget_bytes=1 << 20) as srv:
+        with pytest.raises(MRG8GError):
+            srv.submit(10, 9)                          # unknown kind
+        with pytest.raises(MRG8GError):
+            srv.submit(10, po.U32, generator=3)        # unknown generator
+        with pytest.raises(MRG8GError):
+            srv.submit(1 << 20, po.F64_SHIFTED)        # larger than the budget
+        with pytest.raises(MRG8GError):
+            srv.release(12345)                         # unknown ticket
+        with pytest.raises(MRG8GError):
+            srv.add_generator([0] * 8)                 # all-zero state
+        t = srv.submit(1000, po.U32, seed=3)
+        got = {}
+        drain(srv, 1, got, release=False)
+        srv.release(t)
+        with pytest.raises(MRG8GError):
+            srv.release(t)                             # released twice
+        assert srv.stats()["error"] == 0
