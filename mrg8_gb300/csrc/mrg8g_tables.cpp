@@ -148,14 +148,10 @@ static void build(HostTables& t) {
 }
 
 const HostTables& host_tables() {
-    static HostTables* t = nullptr;
+    static HostTables t;  // static storage: built once, no heap
     static std::once_flag once;
-    std::call_once(once, [] {
-        HostTables* p = new HostTables;
-        build(*p);
-        t = p;
-    });
-    return *t;
+    std::call_once(once, [] { build(t); });
+    return t;
 }
 
 void mcg64ni(uint32_t seed, uint32_t st[8]) {
