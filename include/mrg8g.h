@@ -189,6 +189,29 @@ MRG8G_API int mrg8g_batch_launch(mrg8g_batch *b, void *stream);
  * cuda/mrg8_cuda.cu:414-436), all on `stream`.  Same values as a batch. */
 MRG8G_API int mrg8g_generate_each(const mrg8g_instance *inst, uint64_t count, void *stream);
 
+/* Largest batch accepted by mrg8g_batch_generate_noalloc. */
+#define MRG8G_NOALLOC_MAX_INSTANCES 4096
+#define MRG8G_NOALLOC_MAX_TILES 65536 /* tiles of 512 warp rows (32K-64K outputs each) */
+
+/* Allocation-free form of a batch.  No reference counterpart: the reference
+ * has no batches, and this entry point exists for callers that may not
+ * allocate device memory themselves -- code whose host application or
+ * framework allocator owns all of the GPU's memory, and latency-critical loops
+ * that cannot take cudaMalloc/cudaFree's device-wide synchronisation.  It
+ * generates the same values as mrg8g_batch_create + mrg8g_batch_launch but
+ * calls no cudaMalloc, cudaFree or other allocating routine: the work queue,
+ * instance descriptors and tiles live in a fixed scratch array inside the
+ * library (about 1.3 MB, held on every GPU that loads the library until the
+ * process exits).  The caller still passes the instance array (host memory)
+ * and the output buffers.  Limits: at most MRG8G_NOALLOC_MAX_INSTANCES
+ * instances and MRG8G_NOALLOC_MAX_TILES tiles per call (MRG8G_ERR_BUDGET
+ * beyond).  The first call on a device looks up the scratch array's device
+ * address (and uploads the jump tables if nothing else did), so make that
+ * first call before any stream capture.  All calls share the one array: two
+ * calls whose work overlaps on the GPU (different streams without ordering)
+ * race; calls on the same stream are ordered. */
+MRG8G_API int mrg8g_batch_generate_noalloc(const mrg8g_instance *inst, uint64_t count, void *stream);
+
 /* Time the candidate shapes on this batch (synchronises `stream`), keep the
  * fastest and report it in *chosen (may be NULL). */
 MRG8G_API int mrg8g_batch_autotune(mrg8g_batch *b, void *stream, mrg8g_batch_config *chosen);

@@ -63,6 +63,7 @@ SIGNATURES: dict[str, tuple] = {
     "mrg8g_batch_stats": (_int, [_vp, _vp, _vp, _vp]),
     "mrg8g_batch_destroy": (_int, [_vp]),
     "mrg8g_generate_each": (_int, [_vp, _u64, _vp]),
+    "mrg8g_batch_generate_noalloc": (_int, [_vp, _u64, _vp]),
     "mrg8g_server_create": (_int, [_vp, _vp]),
     "mrg8g_server_add_generator": (_int, [_vp, _vp, _vp]),
     "mrg8g_server_generator_state": (_int, [_vp, _u32, _vp]),

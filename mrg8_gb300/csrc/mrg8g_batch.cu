@@ -9,6 +9,11 @@
 // table and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so
 // every instance's values equal its own sequential stream.  This replaces
 // one mrg8_cuda::mrg8_outer_32 launch per instance (cuda/mrg8_cuda.cu:414-436).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/mrg8g.h"
 #include "mrg8g_device.cuh"
 #include "mrg8g_gen.cuh"
 #include "mrg8g_internal.h"
@@ -88,3 +93,142 @@ int batch_blocks_per_sm(int threads) {
 }
 
 }  // namespace mrg8g
+
+// ---------------------------------------------------------------------------
+// Allocation-free batch entry point (mrg8g_batch_generate_noalloc).
+//
+// Some callers of this library may not allocate device memory themselves:
+// plugins whose host application (or a framework's caching allocator) owns
+// all of the GPU's memory, and latency-critical loops that cannot afford the
+// device-wide synchronisation and unpredictable cost of cudaMalloc/cudaFree.
+// For them the batch path runs from a fixed scratch area that lives in this
+// module as a file-scope device array: the counter of the work queue, the
+// instance descriptors and the tiles.  Every GPU that loads the library holds
+// this array (about 1.3 MB) until the process exits.
+//
+// Layout: [0, 256) work counter | instances (64 B each) | tiles (16 B each).
+namespace mrg8g {
+namespace {
+
+constexpr size_t kNoAllocInstOff = 256;
+constexpr size_t kNoAllocTileOff = kNoAllocInstOff + (size_t)MRG8G_NOALLOC_MAX_INSTANCES * sizeof(BatchInst);
+constexpr size_t kNoAllocBytes = kNoAllocTileOff + (size_t)MRG8G_NOALLOC_MAX_TILES * sizeof(BatchTile);
+static_assert(sizeof(BatchInst) == 64 && sizeof(BatchTile) == 16, "descriptor layout");
+constexpr int kNoAllocTileRows = 512;
+constexpr int kMaxDevices = 64;
+
+}  // namespace
+}  // namespace mrg8g
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[mrg8g::kNoAllocBytes];
+
+namespace mrg8g {
+namespace {
+
+// Host staging laid out like the device array (one copy per call).
+alignas(256) unsigned char g_noalloc_host[kNoAllocBytes];
+std::mutex g_noalloc_mu;
+void* g_noalloc_dev[kMaxDevices];
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the host-side name is only a stand-in, never a device address).
+int noalloc_scratch(int dev, void** out) {
+    if (dev < 0 || dev >= kMaxDevices) return fail(MRG8G_ERR_INVALID_ARGUMENT, "device %d out of range", dev);
+    if (!g_noalloc_dev[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+        g_noalloc_dev[dev] = p;
+    }
+    *out = g_noalloc_dev[dev];
+    return MRG8G_SUCCESS;
+}
+
+// Tiles written straight into the staging area (no heap): heads first, then
+// body tiles; the largest-first order of make_tiles by an in-place sort.
+int noalloc_tiles(const BatchInst* insts, uint32_t count, BatchTile* tiles, uint32_t* ntiles) {
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const BatchInst& in = insts[i];
+        if (in.n == 0) continue;
+        const int elem = kind_elem_bytes(in.kind);
+        const uint64_t T = (uint64_t)kNoAllocTileRows * 32 * (uint64_t)default_layout_V(in.kind);
+        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
+        if (head > in.n) head = in.n;
+        const uint64_t body = (in.n - head + T - 1) / T;
+        if ((uint64_t)k + (head ? 1 : 0) + body > MRG8G_NOALLOC_MAX_TILES)
+            return fail(MRG8G_ERR_BUDGET, "batch needs more than %d tiles (the no-alloc limit)", MRG8G_NOALLOC_MAX_TILES);
+        if (head) tiles[k++] = {0, i, (uint32_t)head | kTileHead};
+        for (uint64_t s = head; s < in.n; s += T) tiles[k++] = {s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)};
+    }
+    std::sort(tiles, tiles + k, [&](const BatchTile& x, const BatchTile& y) {
+        const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(insts[x.inst].kind);
+        const uint64_t by = (uint64_t)(y.len_flags & ~kTileHead) * kind_elem_bytes(insts[y.inst].kind);
+        return bx != by ? bx > by : (x.inst != y.inst ? x.inst < y.inst : x.start < y.start);
+    });
+    *ntiles = k;
+    return MRG8G_SUCCESS;
+}
+
+}  // namespace
+}  // namespace mrg8g
+
+extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t count, void* stream) {
+    using namespace mrg8g;
+    if (count && !inst) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null instance array");
+    if (count > MRG8G_NOALLOC_MAX_INSTANCES)
+        return fail(MRG8G_ERR_BUDGET, "%llu instances exceed the no-alloc limit of %d", (unsigned long long)count,
+                    MRG8G_NOALLOC_MAX_INSTANCES);
+    int dev = 0;
+    int rc = ensure_device(&dev, nullptr);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    void* scratch = nullptr;
+    if ((rc = noalloc_scratch(dev, &scratch))) return rc;
+    BatchInst* h_insts = reinterpret_cast<BatchInst*>(g_noalloc_host + kNoAllocInstOff);
+    BatchTile* h_tiles = reinterpret_cast<BatchTile*>(g_noalloc_host + kNoAllocTileOff);
+    for (uint64_t i = 0; i < count; ++i) {
+        const mrg8g_instance& s = inst[i];
+        if (!kind_valid(s.kind))
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: unknown kind %d", (unsigned long long)i, s.kind);
+        if ((rc = validate_state(s.state))) return rc;
+        const int elem = kind_elem_bytes(s.kind);
+        if (s.n && (!s.out || (uintptr_t)s.out % elem))
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: null or misaligned output", (unsigned long long)i);
+        if (s.n > (1ull << 62) || s.offset > ~0ull - s.n)
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "instance %llu: offset + n overflows", (unsigned long long)i);
+        BatchInst& d = h_insts[i];
+        std::memcpy(d.st, s.state, sizeof(d.st));
+        d.offset = s.offset;
+        d.n = s.n;
+        d.out = s.out;
+        d.kind = s.kind;
+        d.slot1 = 0;
+    }
+    uint32_t ntiles = 0;
+    if ((rc = noalloc_tiles(h_insts, (uint32_t)count, h_tiles, &ntiles))) return rc;
+    if (ntiles == 0) return MRG8G_SUCCESS;
+    // The work counter must start at zero; the array keeps the last call's
+    // contents, so the copy below rewrites it together with the descriptors.
+    std::memset(g_noalloc_host, 0, kNoAllocInstOff);
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned char* d = static_cast<unsigned char*>(scratch);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d, g_noalloc_host, kNoAllocInstOff + count * sizeof(BatchInst), cudaMemcpyHostToDevice,
+                             st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d + kNoAllocTileOff, g_noalloc_host + kNoAllocTileOff, ntiles * sizeof(BatchTile),
+                             cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cuda_fail(e, "copy of the no-alloc descriptors");
+    BatchArgs a;
+    a.insts = reinterpret_cast<const BatchInst*>(d + kNoAllocInstOff);
+    a.tiles = reinterpret_cast<const BatchTile*>(d + kNoAllocTileOff);
+    a.ntiles = ntiles;
+    a.counter = reinterpret_cast<uint32_t*>(d);
+    a.states = nullptr;
+    for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+    const int sms = device_sms();
+    const uint64_t want = (ntiles + 3) / 4;
+    const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * batch_blocks_per_sm(128), want));
+    if ((e = launch_batch(a, 128, blocks, st)) != cudaSuccess) return cuda_fail(e, "launching the no-alloc batch");
+    return MRG8G_SUCCESS;
+}
