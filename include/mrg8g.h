@@ -337,6 +337,15 @@ MRG8G_API int mrg8g_convert(const uint32_t *d_in, void *d_out, uint64_t n, int k
 MRG8G_API int mrg8g_jump_states(const uint32_t st[8], const uint64_t *d_offsets, uint32_t *d_states,
                       uint64_t count, void *stream);
 
+/* The jump table in the reference's file format (jump_matrix.txt, read by
+ * original/mrg8.cpp:85-102): A^(2^j), j = 0..246, one matrix per line,
+ * column-major ((r,c) at index r + 8c).  mrg8g_write_jump_matrix writes the
+ * table this library generates; mrg8g_verify_jump_matrix parses a file and
+ * compares it entry by entry (MRG8G_ERR_INVALID_STATE and *mismatches > 0 if
+ * it differs; mismatches may be NULL). */
+MRG8G_API int mrg8g_write_jump_matrix(const char *path);
+MRG8G_API int mrg8g_verify_jump_matrix(const char *path, uint64_t *mismatches);
+
 /* Description of the last error on the calling thread ("" if none). */
 MRG8G_API const char *mrg8g_last_error(void);
 

@@ -51,6 +51,8 @@ SIGNATURES: dict[str, tuple] = {
     "mrg8g_convert": (_int, [_vp, _vp, _u64, _int, _vp]),
     "mrg8g_jump_states": (_int, [_vp, _vp, _vp, _u64, _vp]),
     "mrg8g_generate_from_state": (_int, [_vp, _u64, _vp, _u64, _int, _vp]),
+    "mrg8g_write_jump_matrix": (_int, [C.c_char_p]),
+    "mrg8g_verify_jump_matrix": (_int, [C.c_char_p, _vp]),
     "mrg8g_seed_state": (_int, [_u32, _vp]),
     "mrg8g_stream_sync": (_int, [_vp]),
     "mrg8g_tune_plain": (_int, [_int, _int, _int]),

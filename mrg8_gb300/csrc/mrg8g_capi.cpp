@@ -382,6 +382,41 @@ int mrg8g_get_plain_tuning(int kind, int* V, int* blocks_per_sm) {
     return MRG8G_SUCCESS;
 }
 
+int mrg8g_write_jump_matrix(const char* path) {
+    if (!path) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null path");
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(MRG8G_ERR_INVALID_ARGUMENT, "cannot open %s for writing", path);
+    const HostTables& t = host_tables();
+    for (int j = 0; j < kNumJump; ++j) {
+        for (int c = 0; c < 8; ++c)
+            for (int r = 0; r < 8; ++r) std::fprintf(f, "%12u", t.jump[j][r * 8 + c]);
+        std::fprintf(f, "\n");
+    }
+    const bool ok = std::fclose(f) == 0;
+    return ok ? MRG8G_SUCCESS : fail(MRG8G_ERR_INVALID_ARGUMENT, "error writing %s", path);
+}
+
+int mrg8g_verify_jump_matrix(const char* path, uint64_t* mismatches) {
+    if (!path) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null path");
+    FILE* f = std::fopen(path, "r");
+    if (!f) return fail(MRG8G_ERR_INVALID_ARGUMENT, "cannot open %s", path);
+    const HostTables& t = host_tables();
+    uint64_t bad = 0;
+    for (int k = 0; k < kNumJump * 64; ++k) {
+        unsigned long v;
+        if (std::fscanf(f, "%lu", &v) != 1) {
+            std::fclose(f);
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "%s: %d numbers, expected %d", path, k, kNumJump * 64);
+        }
+        const int j = k / 64, r = k % 8, c = (k % 64) / 8;  // column-major per matrix
+        bad += v != t.jump[j][r * 8 + c];
+    }
+    std::fclose(f);
+    if (mismatches) *mismatches = bad;
+    if (bad) return fail(MRG8G_ERR_INVALID_STATE, "%s differs from A^(2^j) in %llu entries", path, (unsigned long long)bad);
+    return MRG8G_SUCCESS;
+}
+
 int mrg8g_convert(const uint32_t* d_in, void* d_out, uint64_t n, int kind, void* stream) {
     if (kind == MRG8G_U32 || !kind_valid(kind))
         return fail(MRG8G_ERR_INVALID_ARGUMENT, "convert needs a floating-point kind, got %d", kind);

@@ -122,3 +122,28 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(L, "_lib", None)
     with pytest.raises(OSError, match="no CPU fallback"):
         L.load()
+
+
+def test_jump_matrix_file_round_trip(lib, oracle, tmp_path, kat):
+    """The reference's jump_matrix.txt format: the written table parses to the
+    oracle's table (which the golden digest pins to the reference's file), a
+    corrupted entry is reported, and the reference's own file verifies where
+    it is present."""
+    import hashlib
+    from conftest import REFDIR
+    from mrg8_gb300 import _lib as L
+    path = tmp_path / "jump_matrix.txt"
+    assert lib.mrg8g_write_jump_matrix(str(path).encode()) == 0
+    tab = oracle.read_jump_matrix(str(path))
+    assert np.array_equal(tab, oracle.tab)
+    assert hashlib.sha256(tab.astype(np.uint32).tobytes()).hexdigest() == kat["jump_matrix_txt"]["sha256_u32"]
+    bad = C.c_uint64()
+    assert lib.mrg8g_verify_jump_matrix(str(path).encode(), C.byref(bad)) == 0 and bad.value == 0
+    vals = path.read_text().split()
+    vals[1000] = str(int(vals[1000]) + 1)
+    path.write_text(" ".join(vals))
+    assert lib.mrg8g_verify_jump_matrix(str(path).encode(), C.byref(bad)) == L.ERR_INVALID_STATE
+    assert bad.value == 1
+    ref = os.path.join(REFDIR, "original", "jump_matrix.txt")
+    if os.path.exists(ref):
+        assert lib.mrg8g_verify_jump_matrix(ref.encode(), C.byref(bad)) == 0

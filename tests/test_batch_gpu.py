@@ -152,3 +152,34 @@ def test_batch_edge_cases_and_errors(cuda):
     with pytest.raises(m.MRG8GError):
         m.Batch([(m.seed_state(1), 2**64 - 5, buf, po.F64_SHIFTED)])
     torch.cuda.synchronize()
+
+
+def test_config3_jump_stress(cuda, oracle):
+    """Config 3: 65,536 substreams of one seed, each jumped by an offset drawn
+    uniformly in [0, 2^63), 4,096 uint32 outputs each (2^28 outputs, 1 GiB).
+    Every device post-jump state equals the host jump A^k s, the first eight
+    outputs of every substream continue from that state, and whole substreams
+    of a random subset equal the oracle."""
+    import torch
+
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(20240331)
+    count, n = 65536, 4096
+    st = oracle.seed(13579)
+    offs = rng.integers(0, 2**63, count, dtype=np.int64).astype(np.uint64)
+    out = torch.empty((count, n), dtype=torch.int32, device=cuda)
+    b = m.Batch([(st, int(offs[i]), out[i], po.U32) for i in range(count)])
+    b.launch()
+    d_off = torch.from_numpy(offs.view(np.int64)).to(cuda)
+    states = m.jump_states(st, d_off).cpu().numpy().view(np.uint32)
+    torch.cuda.synchronize()
+    host = out.cpu().numpy().view(np.uint32)
+    for i in range(count):
+        js = oracle.jump_matvec(st, int(offs[i]))
+        assert states[i].tolist() == js.tolist(), i
+        first, _ = oracle.randint(js, 8)
+        assert host[i, :8].tolist() == first.tolist(), i
+    for i in rng.integers(0, count, 300):
+        want, _ = oracle.randint(oracle.jump_matvec(st, int(offs[i])), n)
+        assert np.array_equal(host[i], want), i
+    b.close()
