@@ -141,7 +141,7 @@ def cpu_baseline(n: int, kind: int, min_seconds: float = 3.0):
 
 
 def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, seed: int = 4):
-    """Config 4: `count` generators with distinct seeds, lengths log-uniform in
+    """Uneven batch: `count` generators with distinct seeds, lengths log-uniform in
     [1, 2^max_log2], kinds uniform over fp64/fp32/uint32 (SHIFTED uniforms);
     one autotuned graph-captured batch launch vs one bulk launch per instance.
     Both produce the same values (tests/test_batch_gpu.py)."""
@@ -194,7 +194,7 @@ def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, se
 
 
 def run_served(seconds: float, rate: float = 20_000.0):
-    """Config 5: Poisson arrivals at `rate`/s for `seconds`, offsets uniform in
+    """Serving load: Poisson arrivals at `rate`/s for `seconds`, offsets uniform in
     [0, 2^48), lengths log-uniform in [2^8, 2^26], kinds fp64/fp32/uint32,
     16 GiB admission budget, results released on completion."""
     from mrg8_gb300.serve import Server

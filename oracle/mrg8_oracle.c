@@ -1,7 +1,7 @@
 /*
  * mrg8_oracle.c -- CPU restatement of the MRG8 generator (kenmiura/mrg8).
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+ * TEST INFRASTRUCTURE ONLY: the oracle for the CUDA path and the timed CPU
  * baseline.  The product never links or calls this file.  See mrg8_oracle.h
  * for the reference file:line each function restates.
  */

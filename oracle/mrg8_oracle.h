@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference legs of bench.py may load this code, and only as
- * the checker or as the timed CPU baseline.  The product (mrg8_gb300/) never
+ * the oracle for comparisons or as the timed CPU baseline.  The product (mrg8_gb300/) never
  * calls it; the product path fails loudly when its CUDA library is missing.
  *
  * Each function restates the algorithm of the reference file:line it cites

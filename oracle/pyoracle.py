@@ -7,7 +7,8 @@ sources by ``make -C oracle ref``); those only exist where the reference
 sources were present at build time.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU legs import this
-module, as the checker or the timed CPU baseline.  The product never does.
+module, as the oracle for comparisons or as the timed CPU baseline.  The
+product never does.
 """
 from __future__ import annotations
 

@@ -112,8 +112,8 @@ def test_batch_relaunch_autotune_and_plain_launch_agree(cuda, oracle):
     check_canaries(meta)
 
 
-def test_config4_shape_small(cuda, oracle):
-    """Config 4's distribution at reduced scale: distinct seeds, lengths
+def test_uneven_batch_distribution_small(cuda, oracle):
+    """The uneven-batch distribution at reduced scale: distinct seeds, lengths
     log-uniform in [1, 2^18], dtypes mixed uniformly; every instance equal to
     its own sequential stream."""
     import torch
@@ -154,8 +154,8 @@ def test_batch_edge_cases_and_errors(cuda):
     torch.cuda.synchronize()
 
 
-def test_config3_jump_stress(cuda, oracle):
-    """Config 3: 65,536 substreams of one seed, each jumped by an offset drawn
+def test_jump_stress_65536_substreams(cuda, oracle):
+    """65,536 substreams of one seed, each jumped by an offset drawn
     uniformly in [0, 2^63), 4,096 uint32 outputs each (2^28 outputs, 1 GiB).
     Every device post-jump state equals the host jump A^k s, the first eight
     outputs of every substream continue from that state, and whole substreams

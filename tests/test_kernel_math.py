@@ -15,7 +15,7 @@ P = 2147483647
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def native_check(tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("native") / "check_kernel_math")
     subprocess.run(["g++", "-O2", "-std=c++17", "-I" + CSRC, "-o", exe,
                     os.path.join(ROOT, "tests", "native", "check_kernel_math.cpp"),
@@ -23,14 +23,14 @@ def checker(tmp_path_factory):
     return exe
 
 
-def test_uniform_conversion_exhaustive(checker):
-    r = subprocess.run([checker, "conv"], capture_output=True, text=True, timeout=600)
+def test_uniform_conversion_exhaustive(native_check):
+    r = subprocess.run([native_check, "conv"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad=0" in r.stdout
 
 
 @pytest.mark.parametrize("seed", [13579, 7])
-def test_tables_and_decimated_recurrence(checker, oracle, tmp_path, seed):
+def test_tables_and_decimated_recurrence(native_check, oracle, tmp_path, seed):
     from oracle import pyoracle as po
     st = oracle.seed(seed)
     if seed == 7:  # a state with a zero word and a p word
@@ -38,7 +38,7 @@ def test_tables_and_decimated_recurrence(checker, oracle, tmp_path, seed):
     stream, _ = oracle.generate(st, 128 * 160, po.U32)
     path = tmp_path / "stream.bin"
     stream.tofile(path)
-    r = subprocess.run([checker, "leap", str(path), *[str(int(v)) for v in st]], capture_output=True,
+    r = subprocess.run([native_check, "leap", str(path), *[str(int(v)) for v in st]], capture_output=True,
                        timeout=600)
     assert r.returncode == 0, r.stderr.decode()
     jump = np.frombuffer(r.stdout, dtype=np.uint32).reshape(247, 8, 8)

@@ -45,7 +45,7 @@ def gen_device(g, n, kind, cuda, offset=0, canary=True):
     return buf[offset:offset + n].cpu()
 
 
-def test_config1_known_answers(cuda, kat):
+def test_seed13579_2p24_known_answers(cuda, kat):
     """Plain single stream, seed 13579, 2^24: fp64 rand + the same positions as
     uint32, bit-exact with original/mrg8.cpp (golden digests)."""
     import mrg8_gb300 as m
@@ -167,7 +167,7 @@ def test_states_with_zero_and_p_words(cuda, oracle):
 
 @pytest.mark.parametrize("kind", [po.F64_SHIFTED, po.F64_ORIGINAL, po.F32_SHIFTED, po.U32])
 def test_full_size_2p30(cuda, oracle, kind):
-    """Config 2: 2^30 outputs from one seed, bit-exact with the sequential
+    """2^30 outputs from one seed, bit-exact with the sequential
     stream (the oracle splits it over host threads by jump-ahead)."""
     import os
 
@@ -233,7 +233,7 @@ def test_convert_utility(cuda, oracle):
 
 
 def test_device_jump_states(cuda, oracle):
-    """Config 3 prologue: many substreams jumped by offsets drawn in [0, 2^63),
+    """The jump prologue of 65,536 substreams: offsets drawn in [0, 2^63),
     each device state equal to the host jump A^k s."""
     import mrg8_gb300 as m
     import torch
