@@ -125,14 +125,12 @@ MRG8G_HD uint32_t mod_p64(uint64_t v) {
 //   a = H 2^32 + L == 2H + L (mod p);  s = 2H + L < 3 * 2^32  (one mad.wide);
 //   y = (s mod 2^31) + (s >> 31) = s_lo - (s >> 31) p  in [0, p + 5];
 //   x = y, or y - p when y >= p.
+//
+// The multiply-add is plain 64-bit C++ on both sides: nvcc schedules it
+// better than an inline mad.wide.s32 (fewer companion ALU instructions per
+// product on sm_103a).
 MRG8G_HD uint64_t mad_wide_s32(int32_t a, uint32_t b, uint64_t c) {
-#if defined(__CUDA_ARCH__)
-    uint64_t d;
-    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-    return d;
-#else
     return c + (uint64_t)((int64_t)a * (int64_t)(int32_t)b);
-#endif
 }
 
 MRG8G_HD uint32_t reduce_acc(uint64_t a) {
