@@ -140,7 +140,7 @@ def cpu_baseline(n: int, kind: int, min_seconds: float = 3.0):
     return gs, cores, f"{runs} runs of {n} fp64 SHIFTED samples ({n * 8 >> 20} MiB), first run discarded"
 
 
-def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, seed: int = 4):
+def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, seed: int = 4, tune: bool = True):
     """Uneven batch: `count` generators with distinct seeds, lengths log-uniform in
     [1, 2^max_log2], kinds uniform over fp64/fp32/uint32 (SHIFTED uniforms);
     one autotuned graph-captured batch launch vs one bulk launch per instance.
@@ -165,7 +165,7 @@ def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, se
         total += n
         nbytes += n * out.element_size()
     b = m.Batch(insts)
-    tuned = b.autotune()
+    tuned = b.autotune() if tune else b.config
     stream = torch.cuda.current_stream(dev)
 
     def timed(fn, reps):
@@ -360,7 +360,7 @@ def run_gpu(args) -> None:
                        "kernel argument"}
         del host
 
-    batched = None if args.skip_batch or rank else run_batched(dev)
+    batched = None if args.skip_batch or rank else run_batched(dev, count=args.batch_count, tune=not args.batch_no_tune)
     served = None if args.skip_serve or rank else run_served(args.serve_seconds)
 
     # Spot check of this run's output against the oracle (first 2^20 values).
@@ -409,6 +409,8 @@ def main():
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--batch-count", type=int, default=10_000, help="instances of the batched leg (profiling)")
+    ap.add_argument("--batch-no-tune", action="store_true", help="batched leg with the default config (profiling)")
     ap.add_argument("--n", type=int, default=N_PER_RANK, help="outputs per GPU (profiling of small cases)")
     args = ap.parse_args()
     if args.impl == "reference":

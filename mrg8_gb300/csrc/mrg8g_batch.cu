@@ -28,8 +28,7 @@ __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t
                                          const BatchArgs& a, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     T* out = static_cast<T*>(in.out) + t.start;
-    constexpr int V = sizeof(T) == 8 ? 2 : 4;
-    warp_generate<V, KIND>(g_win, s, out, t.len_flags, a.leap[layout_index(V)], scratch);
+    warp_generate<kBatchLayoutV, KIND>(g_win, s, out, t.len_flags, a.leap[layout_index(kBatchLayoutV)], scratch);
 }
 
 template <int KIND>
@@ -40,7 +39,7 @@ __device__ __forceinline__ void run_head(const BatchInst& in, const BatchTile& t
 
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ BatchArgs a) {
-    __shared__ uint32_t scratch[THREADS / 32][8 * 4 * 32];
+    __shared__ uint32_t scratch[THREADS / 32][8 * kBatchLayoutV * 32];
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
     for (;;) {
@@ -152,7 +151,7 @@ int noalloc_tiles(const BatchInst* insts, uint32_t count, BatchTile* tiles, uint
         const BatchInst& in = insts[i];
         if (in.n == 0) continue;
         const int elem = kind_elem_bytes(in.kind);
-        const uint64_t T = (uint64_t)kNoAllocTileRows * 32 * (uint64_t)default_layout_V(in.kind);
+        const uint64_t T = (uint64_t)kNoAllocTileRows * 32 * (uint64_t)kBatchLayoutV;
         uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
         if (head > in.n) head = in.n;
         const uint64_t body = (in.n - head + T - 1) / T;

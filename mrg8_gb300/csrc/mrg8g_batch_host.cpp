@@ -26,8 +26,7 @@ void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vect
         const BatchInst& in = insts[i];
         if (in.n == 0) continue;
         const int elem = kind_elem_bytes(in.kind);
-        const uint64_t V = (uint64_t)default_layout_V(in.kind);
-        const uint64_t T = (uint64_t)tile_rows * 32 * V;
+        const uint64_t T = (uint64_t)tile_rows * 32 * kBatchLayoutV;
         uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
         if (head > in.n) head = in.n;
         if (head) tiles.push_back({0, i, (uint32_t)head | kTileHead});

@@ -24,6 +24,10 @@ int device_sms();
 int kind_elem_bytes(int kind);
 bool kind_valid(int kind);
 int default_layout_V(int kind);
+// Lane layout of the batch kernel for every kind: two substreams per lane
+// keeps its register count (one kernel holds the code of all five kinds) low
+// enough for eight resident blocks of 128 threads per SM.
+constexpr int kBatchLayoutV = 2;
 int validate_state(const uint32_t st[8]);
 void advance_state(uint32_t st[8], uint64_t n);
 int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, cudaStream_t s, int V);

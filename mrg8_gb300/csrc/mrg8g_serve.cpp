@@ -7,9 +7,11 @@
 // admitted as soon as a stream slot and arena space are free and their work
 // overlaps on the device.  Generator states live in a device table; a draw
 // from a registered generator continues its stream (the host keeps only the
-// position).  Completion times are taken by a host callback enqueued after
-// each batch.  Nothing on the device waits: the kernels are the batch kernel
-// and the scheduler waits on the host with bounded timeouts.
+// position).  Each launch records an event; while launches are in flight the
+// scheduler polls their events (and yields between polls), which takes a
+// completion within about a microsecond of the batch's end, and it blocks on
+// a condition variable only when nothing is in flight.  Nothing on the device
+// waits: the kernels are the batch kernel and every host wait is bounded.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -116,6 +118,7 @@ struct Slot {
     uint32_t* d_counter = nullptr;
     BatchInst* h_insts = nullptr;  // pinned staging
     BatchTile* h_tiles = nullptr;
+    cudaEvent_t done_ev = nullptr;  // recorded after the batch
     size_t tiles_cap = 0;
     std::vector<uint64_t> tickets;
     bool busy = false;
@@ -138,8 +141,6 @@ struct mrg8g_server {
     std::condition_variable cv_sched, cv_done;
     std::deque<uint64_t> pending;  // admission order
     std::deque<uint64_t> completed;
-    std::deque<int> done_slots;
-    std::vector<double> done_times;
     std::unordered_map<uint64_t, Req> reqs;
     uint64_t next_ticket = 1;
     bool stop = false;
@@ -152,16 +153,6 @@ struct mrg8g_server {
 };
 
 namespace {
-
-void CUDART_CB on_slot_done(void* p) {
-    Slot* s = static_cast<Slot*>(p);
-    mrg8g_server* sv = s->server;
-    const double t = now_s();
-    std::lock_guard<std::mutex> lk(sv->mu);
-    sv->done_times[s->idx] = t;
-    sv->done_slots.push_back(s->idx);
-    sv->cv_sched.notify_one();
-}
 
 // Descriptors of the tickets admitted to slot `sl` (lock held).
 void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, std::vector<BatchTile>& tiles) {
@@ -210,36 +201,57 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
         if ((e = launch_batch(a, sv->cfg.threads, blocks, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: batch launch");
     }
-    if ((e = cudaLaunchHostFunc(sl.stream, on_slot_done, &sl)) != cudaSuccess)
-        return cuda_fail(e, "serving: completion callback");
+    if ((e = cudaEventRecord(sl.done_ev, sl.stream)) != cudaSuccess)
+        return cuda_fail(e, "serving: completion event");
     return MRG8G_SUCCESS;
+}
+
+// Requests of a finished slot complete at time t with status rc (lock held).
+void finish_slot(mrg8g_server* sv, Slot& sl, double t, int rc) {
+    for (uint64_t tk : sl.tickets) {
+        Req& q = sv->reqs[tk];
+        q.t_done = t;
+        q.status = rc;
+        q.done = true;
+        sv->completed.push_back(tk);
+        sv->finished++;
+        if (rc == MRG8G_SUCCESS) sv->samples += q.r.n;
+    }
+    sl.tickets.clear();
+    sl.busy = false;
 }
 
 void scheduler(mrg8g_server* sv) {
     cudaSetDevice(sv->dev);
     std::vector<BatchInst> insts;
     std::vector<BatchTile> tiles;
-    std::unique_lock<std::mutex> lk(sv->mu);
-    while (!sv->stop) {
-        // Finished launches: their requests complete with the callback time.
-        bool any_done = false;
-        while (!sv->done_slots.empty()) {
-            Slot& sl = sv->slots[sv->done_slots.front()];
-            sv->done_slots.pop_front();
-            const double t = sv->done_times[sl.idx];
-            for (uint64_t tk : sl.tickets) {
-                Req& q = sv->reqs[tk];
-                q.t_done = t;
-                q.done = true;
-                sv->completed.push_back(tk);
-                sv->finished++;
-                sv->samples += q.r.n;
-            }
-            sl.tickets.clear();
-            sl.busy = false;
-            any_done = true;
+    struct Done {
+        int idx;
+        double t;
+        cudaError_t e;
+    };
+    std::vector<Done> done;
+    for (;;) {
+        // In-flight launches, polled without the lock (the scheduler thread
+        // owns the slots while they are busy).
+        done.clear();
+        for (Slot& sl : sv->slots) {
+            if (!sl.busy) continue;
+            const cudaError_t q = cudaEventQuery(sl.done_ev);
+            if (q != cudaErrorNotReady) done.push_back({sl.idx, now_s(), q});
         }
-        if (any_done) sv->cv_done.notify_all();
+        std::unique_lock<std::mutex> lk(sv->mu);
+        if (sv->stop) break;
+        for (const Done& d : done) {
+            int rc = MRG8G_SUCCESS;
+            if (d.e != cudaSuccess) {
+                rc = cuda_fail(d.e, "serving: batch execution");
+                sv->error = rc;
+                sv->error_msg = mrg8g_last_error();
+            }
+            finish_slot(sv, sv->slots[d.idx], d.t, rc);
+        }
+        if (!done.empty()) sv->cv_done.notify_all();
         // Admission into free slots, first in first out.
         for (Slot& sl : sv->slots) {
             if (sl.busy || sv->pending.empty() || sv->error) continue;
@@ -264,19 +276,18 @@ void scheduler(mrg8g_server* sv) {
             if (rc) {
                 sv->error = rc;
                 sv->error_msg = msg;
-                for (uint64_t tk : sl.tickets) {
-                    Req& q = sv->reqs[tk];
-                    q.status = rc;
-                    q.done = true;
-                    q.t_done = now_s();
-                    sv->completed.push_back(tk);
-                }
-                sl.tickets.clear();
-                sl.busy = false;
+                finish_slot(sv, sl, now_s(), rc);
                 sv->cv_done.notify_all();
             }
         }
-        sv->cv_sched.wait_for(lk, std::chrono::microseconds(500));
+        bool inflight = false;
+        for (const Slot& sl : sv->slots) inflight |= sl.busy;
+        if (inflight) {
+            lk.unlock();
+            std::this_thread::yield();
+        } else {
+            sv->cv_sched.wait_for(lk, std::chrono::microseconds(500));
+        }
     }
 }
 
@@ -296,6 +307,7 @@ void destroy_server(mrg8g_server* sv) {
         if (sl.d_counter) cudaFree(sl.d_counter);
         if (sl.h_insts) cudaFreeHost(sl.h_insts);
         if (sl.h_tiles) cudaFreeHost(sl.h_tiles);
+        if (sl.done_ev) cudaEventDestroy(sl.done_ev);
     }
     if (sv->arena_base) cudaFree(sv->arena_base);
     if (sv->d_states) cudaFree(sv->d_states);
@@ -337,12 +349,12 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
         destroy_server(sv);
         return cuda_fail(e, "serving: arena allocation");
     }
-    // Tiles per launch are bounded by the arena (every tile but a head covers
-    // at least one row, and a full tile covers tile_rows * 512 bytes).
-    const size_t min_tile_bytes = (size_t)c.tile_rows * 32 * 4 * 4;
+    // Tiles per launch are bounded by the arena: an instance has at most one
+    // head and one partial tile, and a full tile covers tile_rows rows of
+    // 32 * kBatchLayoutV elements of at least 4 bytes.
+    const size_t min_tile_bytes = (size_t)c.tile_rows * 32 * kBatchLayoutV * 4;
     const size_t tiles_cap = c.budget_bytes / min_tile_bytes + 3 * (size_t)c.max_batch + 16;
     sv->slots.resize(c.inflight);
-    sv->done_times.assign(c.inflight, 0.0);
     for (uint32_t i = 0; i < c.inflight; ++i) {
         Slot& sl = sv->slots[i];
         sl.idx = (int)i;
@@ -353,7 +365,8 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
             (e = cudaMalloc(&sl.d_tiles, tiles_cap * sizeof(BatchTile))) != cudaSuccess ||
             (e = cudaMalloc(&sl.d_counter, sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaHostAlloc(&sl.h_insts, c.max_batch * sizeof(BatchInst), cudaHostAllocDefault)) != cudaSuccess ||
-            (e = cudaHostAlloc(&sl.h_tiles, tiles_cap * sizeof(BatchTile), cudaHostAllocDefault)) != cudaSuccess) {
+            (e = cudaHostAlloc(&sl.h_tiles, tiles_cap * sizeof(BatchTile), cudaHostAllocDefault)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess) {
             destroy_server(sv);
             return cuda_fail(e, "serving: slot allocation");
         }
