@@ -74,6 +74,15 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
         default: run_tile<kF32Shift>(in, t, s, a, sc); break;
         }
     }
+    // Self-resetting queue: once every block has left the loop, no warp
+    // reads the counter again in this launch.
+    if (a.done_blocks) {
+        __syncthreads();
+        if (threadIdx.x == 0 && atomicAdd(a.done_blocks, 1u) == gridDim.x - 1) {
+            *a.counter = 0;
+            *a.done_blocks = 0;
+        }
+    }
 }
 
 cudaError_t launch_batch(const BatchArgs& a, int threads, int blocks, cudaStream_t st) {
@@ -223,6 +232,7 @@ extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t
     a.tiles = reinterpret_cast<const BatchTile*>(d + kNoAllocTileOff);
     a.ntiles = ntiles;
     a.counter = reinterpret_cast<uint32_t*>(d);
+    a.done_blocks = nullptr;
     a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     const int sms = device_sms();

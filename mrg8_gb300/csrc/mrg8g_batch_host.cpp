@@ -123,6 +123,7 @@ BatchArgs args_of(const mrg8g_batch* b) {
     a.tiles = b->d_tiles;
     a.ntiles = (uint32_t)b->tiles.size();
     a.counter = b->d_counter;
+    a.done_blocks = nullptr;
     a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     return a;

@@ -55,6 +55,8 @@ struct BatchArgs {
     const BatchTile* tiles;
     uint32_t ntiles;
     uint32_t* counter;        // work-queue position, zero before each launch
+    uint32_t* done_blocks;    // null, or blocks finished: the last block then
+                              // zeroes *counter and *done_blocks for the next launch
     const uint32_t* states;   // generator table (8 words per slot) or null
     LeapCoef leap[kNumLayouts];
 };

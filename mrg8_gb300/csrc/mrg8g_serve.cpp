@@ -113,11 +113,9 @@ struct Req {
 struct Slot {
     int idx = 0;
     cudaStream_t stream = nullptr;
-    BatchInst* d_insts = nullptr;
-    BatchTile* d_tiles = nullptr;
-    uint32_t* d_counter = nullptr;
-    BatchInst* h_insts = nullptr;  // pinned staging
-    BatchTile* h_tiles = nullptr;
+    char* d_stage = nullptr;        // instances, then tiles (one copy per launch)
+    char* h_stage = nullptr;        // pinned staging of the same layout
+    uint32_t* d_counter = nullptr;  // work-queue counter, finished-block counter
     cudaEvent_t done_ev = nullptr;  // recorded after the batch
     size_t tiles_cap = 0;
     std::vector<uint64_t> tickets;
@@ -139,11 +137,12 @@ struct mrg8g_server {
 
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
+    std::atomic<uint64_t> wake_seq{0};  // bumped by submissions and releases
+    std::atomic<bool> stop{false};
     std::deque<uint64_t> pending;  // admission order
     std::deque<uint64_t> completed;
     std::unordered_map<uint64_t, Req> reqs;
     uint64_t next_ticket = 1;
-    bool stop = false;
     int error = MRG8G_SUCCESS;
     std::string error_msg;
     std::thread thread;
@@ -176,23 +175,19 @@ void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, st
 int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts, const std::vector<BatchTile>& tiles) {
     const size_t count = insts.size();
     if (tiles.size() > sl.tiles_cap) return fail(MRG8G_ERR_BUDGET, "batch needs %zu tiles (cap %zu)", tiles.size(), sl.tiles_cap);
-    std::memcpy(sl.h_insts, insts.data(), count * sizeof(BatchInst));
-    std::memcpy(sl.h_tiles, tiles.data(), tiles.size() * sizeof(BatchTile));
+    const size_t ib = count * sizeof(BatchInst), tb = tiles.size() * sizeof(BatchTile);
+    std::memcpy(sl.h_stage, insts.data(), ib);
+    std::memcpy(sl.h_stage + ib, tiles.data(), tb);
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(sl.d_insts, sl.h_insts, count * sizeof(BatchInst), cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
-        return cuda_fail(e, "serving: copy of instances");
-    if (!tiles.empty() &&
-        (e = cudaMemcpyAsync(sl.d_tiles, sl.h_tiles, tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
-                             sl.stream)) != cudaSuccess)
-        return cuda_fail(e, "serving: copy of tiles");
-    if ((e = cudaMemsetAsync(sl.d_counter, 0, sizeof(uint32_t), sl.stream)) != cudaSuccess)
-        return cuda_fail(e, "serving: counter reset");
     if (!tiles.empty()) {
+        if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + tb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
+            return cuda_fail(e, "serving: copy of the batch descriptors");
         BatchArgs a;
-        a.insts = sl.d_insts;
-        a.tiles = sl.d_tiles;
+        a.insts = reinterpret_cast<const BatchInst*>(sl.d_stage);
+        a.tiles = reinterpret_cast<const BatchTile*>(sl.d_stage + ib);
         a.ntiles = (uint32_t)tiles.size();
         a.counter = sl.d_counter;
+        a.done_blocks = sl.d_counter + 1;  // the kernel leaves both at zero
         a.states = sv->d_states;
         for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
         const uint64_t wpb = (uint64_t)sv->cfg.threads / 32;
@@ -221,6 +216,11 @@ void finish_slot(mrg8g_server* sv, Slot& sl, double t, int rc) {
     sl.busy = false;
 }
 
+// The scheduler spins (yielding) while launches are in flight and for
+// kSpinIdle seconds after the last activity, so that requests arriving at a
+// steady rate find it awake; after that it sleeps on cv_sched.
+constexpr double kSpinIdle = 2e-3;
+
 void scheduler(mrg8g_server* sv) {
     cudaSetDevice(sv->dev);
     std::vector<BatchInst> insts;
@@ -231,7 +231,10 @@ void scheduler(mrg8g_server* sv) {
         cudaError_t e;
     };
     std::vector<Done> done;
-    for (;;) {
+    uint64_t seen = ~0ull;
+    double active = now_s();
+    bool inflight = false;
+    while (!sv->stop.load(std::memory_order_acquire)) {
         // In-flight launches, polled without the lock (the scheduler thread
         // owns the slots while they are busy).
         done.clear();
@@ -240,8 +243,21 @@ void scheduler(mrg8g_server* sv) {
             const cudaError_t q = cudaEventQuery(sl.done_ev);
             if (q != cudaErrorNotReady) done.push_back({sl.idx, now_s(), q});
         }
+        const uint64_t ws = sv->wake_seq.load(std::memory_order_acquire);
+        if (done.empty() && ws == seen) {  // nothing new
+            if (inflight || now_s() - active < kSpinIdle) {
+                std::this_thread::yield();
+                continue;
+            }
+            std::unique_lock<std::mutex> lk(sv->mu);
+            sv->cv_sched.wait_for(lk, std::chrono::microseconds(500), [&] {
+                return sv->stop.load(std::memory_order_relaxed) || sv->wake_seq.load(std::memory_order_relaxed) != seen;
+            });
+            continue;
+        }
+        seen = ws;
+        active = now_s();
         std::unique_lock<std::mutex> lk(sv->mu);
-        if (sv->stop) break;
         for (const Done& d : done) {
             int rc = MRG8G_SUCCESS;
             if (d.e != cudaSuccess) {
@@ -280,14 +296,8 @@ void scheduler(mrg8g_server* sv) {
                 sv->cv_done.notify_all();
             }
         }
-        bool inflight = false;
+        inflight = false;
         for (const Slot& sl : sv->slots) inflight |= sl.busy;
-        if (inflight) {
-            lk.unlock();
-            std::this_thread::yield();
-        } else {
-            sv->cv_sched.wait_for(lk, std::chrono::microseconds(500));
-        }
     }
 }
 
@@ -295,18 +305,16 @@ void destroy_server(mrg8g_server* sv) {
     if (sv->thread.joinable()) {
         {
             std::lock_guard<std::mutex> lk(sv->mu);
-            sv->stop = true;
+            sv->stop.store(true, std::memory_order_release);
             sv->cv_sched.notify_all();
         }
         sv->thread.join();
     }
     for (Slot& sl : sv->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream), cudaStreamDestroy(sl.stream);
-        if (sl.d_insts) cudaFree(sl.d_insts);
-        if (sl.d_tiles) cudaFree(sl.d_tiles);
+        if (sl.d_stage) cudaFree(sl.d_stage);
         if (sl.d_counter) cudaFree(sl.d_counter);
-        if (sl.h_insts) cudaFreeHost(sl.h_insts);
-        if (sl.h_tiles) cudaFreeHost(sl.h_tiles);
+        if (sl.h_stage) cudaFreeHost(sl.h_stage);
         if (sl.done_ev) cudaEventDestroy(sl.done_ev);
     }
     if (sv->arena_base) cudaFree(sv->arena_base);
@@ -360,12 +368,12 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
         sl.idx = (int)i;
         sl.server = sv;
         sl.tiles_cap = tiles_cap;
+        const size_t stage = c.max_batch * sizeof(BatchInst) + tiles_cap * sizeof(BatchTile);
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
-            (e = cudaMalloc(&sl.d_insts, c.max_batch * sizeof(BatchInst))) != cudaSuccess ||
-            (e = cudaMalloc(&sl.d_tiles, tiles_cap * sizeof(BatchTile))) != cudaSuccess ||
-            (e = cudaMalloc(&sl.d_counter, sizeof(uint32_t))) != cudaSuccess ||
-            (e = cudaHostAlloc(&sl.h_insts, c.max_batch * sizeof(BatchInst), cudaHostAllocDefault)) != cudaSuccess ||
-            (e = cudaHostAlloc(&sl.h_tiles, tiles_cap * sizeof(BatchTile), cudaHostAllocDefault)) != cudaSuccess ||
+            (e = cudaMalloc(&sl.d_stage, stage)) != cudaSuccess ||
+            (e = cudaMalloc(&sl.d_counter, 2 * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMemset(sl.d_counter, 0, 2 * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaHostAlloc(&sl.h_stage, stage, cudaHostAllocDefault)) != cudaSuccess ||
             (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess) {
             destroy_server(sv);
             return cuda_fail(e, "serving: slot allocation");
@@ -439,6 +447,7 @@ int mrg8g_server_submit(mrg8g_server* sv, const mrg8g_request* r, uint64_t* tick
     sv->reqs.emplace(tk, q);
     sv->pending.push_back(tk);
     sv->submitted++;
+    sv->wake_seq.fetch_add(1, std::memory_order_release);
     sv->cv_sched.notify_one();
     *ticket = tk;
     return MRG8G_SUCCESS;
@@ -495,6 +504,7 @@ int mrg8g_server_release(mrg8g_server* sv, uint64_t ticket) {
     if (!it->second.done) return fail(MRG8G_ERR_NOT_READY, "ticket %llu is not complete", (unsigned long long)ticket);
     if (it->second.t_admit > 0) sv->arena->release(it->second.arena_off);
     sv->reqs.erase(it);
+    sv->wake_seq.fetch_add(1, std::memory_order_release);
     sv->cv_sched.notify_one();
     return MRG8G_SUCCESS;
 }
