@@ -236,7 +236,9 @@ typedef struct mrg8g_server_config {
     uint32_t max_batch;      /* requests per launch at most (0: 1024)        */
     uint32_t inflight;       /* launches in flight, one stream each (0: 3)   */
     uint32_t max_generators; /* device-resident generator slots (0: 65536)   */
-    int32_t tile_rows;       /* batch-kernel tile rows (0: 256)              */
+    int32_t tile_rows;       /* batch-kernel tile rows at most (0: 256); a
+                                launch too small to fill the GPU with such
+                                tiles uses shorter ones (16 rows at least)  */
     int32_t threads;         /* batch-kernel block size, 128 or 256 (0: 128) */
     int32_t reserved;        /* 0                                            */
 } mrg8g_server_config;

@@ -32,14 +32,56 @@ __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t
 }
 
 template <int KIND>
-__device__ __forceinline__ void run_head(const BatchInst& in, const BatchTile& t, uint32_t s[8]) {
+__device__ __forceinline__ void run_head(const BatchInst& in, const BatchTile& t, uint32_t s[8],
+                                         const uint32_t* jump) {
     using T = typename OutOf<KIND>::T;
-    lane_sequential<KIND>(g_jump, s, static_cast<T*>(in.out) + t.start, t.len_flags & ~kTileHead);
+    lane_sequential<KIND>(jump, s, static_cast<T*>(in.out) + t.start, t.len_flags & ~kTileHead);
+}
+
+// Instance owning tile ti of a device-tiled launch: the largest i with
+// tile_base[i] <= ti, found by a 32-way search (one load per lane per level,
+// one level for up to 32 instances).  Called by all 32 lanes with the same ti.
+__device__ __forceinline__ uint32_t tile_owner(const uint32_t* __restrict__ base, uint32_t ninst, uint32_t ti) {
+    const int lane = threadIdx.x & 31;
+    uint32_t lo = 0, hi = ninst;  // base[lo] <= ti < base[hi]
+    while (hi - lo > 1) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t c = lo + (uint32_t)lane * step;
+        const unsigned m = __ballot_sync(kFull, c < hi && base[c] <= ti);
+        lo += (uint32_t)(31 - __clz((int)m)) * step;
+        hi = min(hi, lo + step);
+    }
+    return lo;
+}
+
+// Tile ti of a device-tiled launch (see BatchArgs).
+__device__ __forceinline__ BatchTile derive_tile(const BatchArgs& a, uint32_t ti, const BatchInst& in, uint32_t i) {
+    const uint32_t elem = (in.kind == kF64Orig || in.kind == kF64Shift) ? 8u : 4u;
+    uint64_t head = ((16u - (uint32_t)((uintptr_t)in.out & 15u)) & 15u) / elem;
+    if (head > in.n) head = in.n;
+    const uint32_t li = ti - a.tile_base[i];
+    BatchTile t;
+    t.inst = i;
+    if (head && li == 0) {
+        t.start = 0;
+        t.len_flags = (uint32_t)head | kTileHead;
+    } else {
+        t.start = head + (uint64_t)(li - (head ? 1u : 0u)) * a.tile_elems;
+        const uint64_t left = in.n - t.start;
+        t.len_flags = (uint32_t)(left < a.tile_elems ? left : a.tile_elems);
+    }
+    return t;
 }
 
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ BatchArgs a) {
     __shared__ uint32_t scratch[THREADS / 32][8 * kBatchLayoutV * 32];
+    // The A^(2^i) table in shared memory: a block's tiles jump from here
+    // instead of from L2, whose latency a short tile cannot hide.
+    __shared__ __align__(16) uint32_t sjump[kDevJump * 64];
+    for (int q = threadIdx.x; q < kDevJump * 16; q += THREADS)
+        reinterpret_cast<uint4*>(sjump)[q] = reinterpret_cast<const uint4*>(g_jump)[q];
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
     for (;;) {
@@ -47,21 +89,29 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
         if (lane == 0) ti = atomicAdd(a.counter, 1u);
         ti = __shfl_sync(kFull, ti, 0);
         if (ti >= a.ntiles) break;
-        const BatchTile t = a.tiles[ti];
-        const BatchInst in = a.insts[t.inst];
+        BatchTile t;
+        BatchInst in;
+        if (a.tiles) {
+            t = a.tiles[ti];
+            in = a.insts[t.inst];
+        } else {
+            const uint32_t i = tile_owner(a.tile_base, a.ninst, ti);
+            in = a.insts[i];
+            t = derive_tile(a, ti, in, i);
+        }
         const uint32_t* src = in.slot1 ? a.states + 8ull * (in.slot1 - 1) : in.st;
         uint32_t s[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) s[q] = src[q];
-        warp_jump(g_jump, s, in.offset + t.start);
+        warp_jump(sjump, s, in.offset + t.start);
         if (t.len_flags & kTileHead) {
             if (lane == 0) {
                 switch (in.kind) {
-                case kU32: run_head<kU32>(in, t, s); break;
-                case kF64Orig: run_head<kF64Orig>(in, t, s); break;
-                case kF64Shift: run_head<kF64Shift>(in, t, s); break;
-                case kF32Orig: run_head<kF32Orig>(in, t, s); break;
-                default: run_head<kF32Shift>(in, t, s); break;
+                case kU32: run_head<kU32>(in, t, s, sjump); break;
+                case kF64Orig: run_head<kF64Orig>(in, t, s, sjump); break;
+                case kF64Shift: run_head<kF64Shift>(in, t, s, sjump); break;
+                case kF32Orig: run_head<kF32Orig>(in, t, s, sjump); break;
+                default: run_head<kF32Shift>(in, t, s, sjump); break;
                 }
             }
             continue;
@@ -85,13 +135,29 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
     }
 }
 
+// Shared memory before L1: the blocks of k_batch hold the jump table.
+static cudaError_t prefer_shared() {
+    static cudaError_t e = [] {
+        cudaError_t r = cudaFuncSetAttribute(k_batch<128>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             (int)cudaSharedmemCarveoutMaxShared);
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(k_batch<256>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
+        return r;
+    }();
+    return e;
+}
+
 cudaError_t launch_batch(const BatchArgs& a, int threads, int blocks, cudaStream_t st) {
+    cudaError_t e = prefer_shared();
+    if (e != cudaSuccess) return e;
     if (threads == 256) k_batch<256><<<blocks, 256, 0, st>>>(a);
     else k_batch<128><<<blocks, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 int batch_blocks_per_sm(int threads) {
+    if (prefer_shared() != cudaSuccess) return 1;
     int nb = 0;
     cudaError_t e = threads == 256
                         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<256>, 256, 0)
@@ -233,6 +299,9 @@ extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t
     a.ntiles = ntiles;
     a.counter = reinterpret_cast<uint32_t*>(d);
     a.done_blocks = nullptr;
+    a.tile_base = nullptr;
+    a.ninst = count;
+    a.tile_elems = 0;
     a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     const int sms = device_sms();

@@ -124,6 +124,9 @@ BatchArgs args_of(const mrg8g_batch* b) {
     a.ntiles = (uint32_t)b->tiles.size();
     a.counter = b->d_counter;
     a.done_blocks = nullptr;
+    a.tile_base = nullptr;
+    a.ninst = (uint32_t)b->insts.size();
+    a.tile_elems = 0;
     a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     return a;

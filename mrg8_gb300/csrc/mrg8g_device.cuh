@@ -62,10 +62,13 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uin
     uint32_t a0 = c0 == 0 ? s[0] : c0 == 2 ? s[2] : c0 == 4 ? s[4] : s[6];
     uint32_t a1 = c0 == 0 ? s[1] : c0 == 2 ? s[3] : c0 == 4 ? s[5] : s[7];
     uint32_t val = 0;
-    while (k) {
-        const int i = __ffsll((long long)k) - 1;
+    // The next matrix's entries are loaded before the current product's
+    // shuffles, so that a load's latency overlaps one step.
+    uint2 m = reinterpret_cast<const uint2*>(jump + (__ffsll((long long)k) - 1) * 64)[lane];
+    for (;;) {
         k &= k - 1;
-        const uint2 m = __ldg(reinterpret_cast<const uint2*>(jump + i * 64) + lane);
+        uint2 mn = make_uint2(0u, 0u);
+        if (k) mn = reinterpret_cast<const uint2*>(jump + (__ffsll((long long)k) - 1) * 64)[lane];
         const uint64_t part = (uint64_t)m.x * a0 + (uint64_t)m.y * a1;  // < 2^63
         uint64_t f = (part & kP) + (part >> 31);                        // < 2^33
         f += __shfl_xor_sync(kFull, f, 1);
@@ -73,6 +76,8 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uin
         val = mod_p64(f);
         a0 = __shfl_sync(kFull, val, c0 << 2);
         a1 = __shfl_sync(kFull, val, (c0 << 2) + 4);
+        if (!k) break;
+        m = mn;
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = __shfl_sync(kFull, val, q << 2);
@@ -80,7 +85,8 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uin
 
 // Initial window of a lane for layout V: x[v][j] = S[B + V lane + v + d j] - 1
 // for j = 0..7 (d = 32 V), from the state s taken at stream position B.  The
-// 8 V dot products run one at a time (keeping the setup's register peak
+// 8 V dot products run four at a time (the four table rows are loaded
+// together, so their latencies overlap, and the setup's register peak stays
 // below the main loop's) through the warp's scratch rows in shared memory,
 // `scratch` holding 8 V * 32 words laid out [slot][lane].
 template <int V>
@@ -88,13 +94,22 @@ __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, co
                                             int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
     const uint32_t* w = win + win_offset(layout_index(V));
 #pragma unroll 1
-    for (int i = 0; i < 8 * V; ++i) {
-        const int v = i >> 3, j = i & 7;
-        const uint4* row = reinterpret_cast<const uint4*>(w + ((V * lane + v) * 8 + j) * 8);
-        const uint4 r0 = __ldg(row), r1 = __ldg(row + 1);
-        const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-        const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
-        scratch[i * 32 + lane] = (S ? S : kP) - 1u;
+    for (int i0 = 0; i0 < 8 * V; i0 += 4) {
+        uint4 r[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + q, v = i >> 3, j = i & 7;
+            const uint4* row = reinterpret_cast<const uint4*>(w + ((V * lane + v) * 8 + j) * 8);
+            r[2 * q] = __ldg(row);
+            r[2 * q + 1] = __ldg(row + 1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 r0 = r[2 * q], r1 = r[2 * q + 1];
+            const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+            const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
+            scratch[(i0 + q) * 32 + lane] = (S ? S : kP) - 1u;
+        }
     }
 #pragma unroll
     for (int v = 0; v < V; ++v)

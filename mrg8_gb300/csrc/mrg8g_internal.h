@@ -50,9 +50,16 @@ struct BatchTile {
     uint32_t len_flags;
 };
 
+// Tiles are either listed by the host (`tiles`) or, when `tiles` is null,
+// derived on the device: instance i owns tiles [tile_base[i], tile_base[i+1])
+// of the launch, its head (outputs before the first 16-byte boundary of its
+// buffer, if any) and then body tiles of `tile_elems` outputs.
 struct BatchArgs {
     const BatchInst* insts;
     const BatchTile* tiles;
+    const uint32_t* tile_base;  // ninst + 1 prefix counts, used when tiles is null
+    uint32_t ninst;
+    uint32_t tile_elems;        // body tile length (a multiple of 32 * kBatchLayoutV)
     uint32_t ntiles;
     uint32_t* counter;        // work-queue position, zero before each launch
     uint32_t* done_blocks;    // null, or blocks finished: the last block then

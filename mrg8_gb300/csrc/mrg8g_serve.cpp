@@ -2,7 +2,8 @@
 //
 // A scheduler thread admits requests first-in first-out against a device
 // output arena (the admission budget), packs the admitted ones into a batch
-// (the tiles of the batch kernel, mrg8g_batch.cu) and launches it on one of
+// (the batch kernel of mrg8g_batch.cu, deriving its tiles on the device from
+// the requests' tile counts) and launches it on one of
 // several streams, so that requests arriving while others are on the GPU are
 // admitted as soon as a stream slot and arena space are free and their work
 // overlaps on the device.  Generator states live in a device table; a draw
@@ -113,11 +114,10 @@ struct Req {
 struct Slot {
     int idx = 0;
     cudaStream_t stream = nullptr;
-    char* d_stage = nullptr;        // instances, then tiles (one copy per launch)
+    char* d_stage = nullptr;        // instances, then tile prefix counts (one copy per launch)
     char* h_stage = nullptr;        // pinned staging of the same layout
     uint32_t* d_counter = nullptr;  // work-queue counter, finished-block counter
     cudaEvent_t done_ev = nullptr;  // recorded after the batch
-    size_t tiles_cap = 0;
     std::vector<uint64_t> tickets;
     bool busy = false;
     mrg8g_server* server = nullptr;
@@ -153,10 +153,25 @@ struct mrg8g_server {
 
 namespace {
 
-// Descriptors of the tickets admitted to slot `sl` (lock held).
-void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, std::vector<BatchTile>& tiles) {
+// Fewest rows per tile of a serving launch.  Below about this many rows the
+// per-tile jump of the state costs more than generating the tile.
+constexpr uint64_t kMinServeTileRows = 16;
+
+// Resident warps of one batch launch.
+uint64_t launch_warps(const mrg8g_server* sv) { return (uint64_t)sv->sms * sv->bps * (sv->cfg.threads / 32); }
+
+// Descriptors of the tickets admitted to slot `sl` (lock held): the
+// instances, largest first, and the prefix counts of their tiles, which the
+// batch kernel turns into tiles itself.  Rows per tile: as many as spread
+// the launch's rows over the resident warps, between kMinServeTileRows and
+// the configured maximum, so that a request that would not fill the GPU with
+// full tiles still runs on many warps at once.
+void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, std::vector<uint32_t>& base,
+                   uint32_t* tile_elems) {
     const uint32_t count = (uint32_t)sl.tickets.size();
     insts.resize(count);
+    constexpr uint64_t D = 32 * kBatchLayoutV;
+    uint64_t rows = 0;
     for (uint32_t i = 0; i < count; ++i) {
         const Req& q = sv->reqs[sl.tickets[i]];
         BatchInst& d = insts[i];
@@ -166,32 +181,55 @@ void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, st
         d.out = static_cast<char*>(sv->arena_base) + q.arena_off;
         d.kind = q.r.kind;
         d.slot1 = q.r.generator == MRG8G_NO_GENERATOR ? 0u : q.r.generator + 1u;
+        rows += (d.n + D - 1) / D;
     }
-    make_tiles(insts.data(), count, sv->cfg.tile_rows, tiles);
+    std::stable_sort(insts.begin(), insts.end(), [](const BatchInst& x, const BatchInst& y) {
+        return x.n * kind_elem_bytes(x.kind) > y.n * kind_elem_bytes(y.kind);
+    });
+    const uint64_t warps = launch_warps(sv);
+    uint64_t tr = ((rows + warps - 1) / warps + 7) / 8 * 8;
+    tr = std::min<uint64_t>(std::max<uint64_t>(tr, kMinServeTileRows), (uint64_t)sv->cfg.tile_rows);
+    const uint64_t T = tr * D;
+    *tile_elems = (uint32_t)T;
+    base.resize(count + 1);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        base[i] = (uint32_t)total;
+        const BatchInst& d = insts[i];
+        if (!d.n) continue;
+        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
+        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
+        total += (head ? 1 : 0) + (d.n - head + T - 1) / T;
+    }
+    base[count] = (uint32_t)total;
 }
 
 // Enqueue slot `sl`'s batch on its stream (lock not held; the slot is owned
 // by the scheduler thread while busy).
-int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts, const std::vector<BatchTile>& tiles) {
+int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts, const std::vector<uint32_t>& base,
+                 uint32_t tile_elems) {
     const size_t count = insts.size();
-    if (tiles.size() > sl.tiles_cap) return fail(MRG8G_ERR_BUDGET, "batch needs %zu tiles (cap %zu)", tiles.size(), sl.tiles_cap);
-    const size_t ib = count * sizeof(BatchInst), tb = tiles.size() * sizeof(BatchTile);
+    const uint32_t ntiles = base[count];
+    const size_t ib = count * sizeof(BatchInst), bb = (count + 1) * sizeof(uint32_t);
     std::memcpy(sl.h_stage, insts.data(), ib);
-    std::memcpy(sl.h_stage + ib, tiles.data(), tb);
+    std::memcpy(sl.h_stage + ib, base.data(), bb);
     cudaError_t e;
-    if (!tiles.empty()) {
-        if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + tb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
+    if (ntiles) {
+        if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + bb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: copy of the batch descriptors");
         BatchArgs a;
         a.insts = reinterpret_cast<const BatchInst*>(sl.d_stage);
-        a.tiles = reinterpret_cast<const BatchTile*>(sl.d_stage + ib);
-        a.ntiles = (uint32_t)tiles.size();
+        a.tiles = nullptr;
+        a.tile_base = reinterpret_cast<const uint32_t*>(sl.d_stage + ib);
+        a.ninst = (uint32_t)count;
+        a.tile_elems = tile_elems;
+        a.ntiles = ntiles;
         a.counter = sl.d_counter;
         a.done_blocks = sl.d_counter + 1;  // the kernel leaves both at zero
         a.states = sv->d_states;
         for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
         const uint64_t wpb = (uint64_t)sv->cfg.threads / 32;
-        const uint64_t want = (tiles.size() + wpb - 1) / wpb;
+        const uint64_t want = (ntiles + wpb - 1) / wpb;
         const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sv->sms * sv->bps, want));
         if ((e = launch_batch(a, sv->cfg.threads, blocks, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: batch launch");
@@ -224,7 +262,8 @@ constexpr double kSpinIdle = 2e-3;
 void scheduler(mrg8g_server* sv) {
     cudaSetDevice(sv->dev);
     std::vector<BatchInst> insts;
-    std::vector<BatchTile> tiles;
+    std::vector<uint32_t> base;
+    uint32_t tile_elems = 0;
     struct Done {
         int idx;
         double t;
@@ -281,12 +320,12 @@ void scheduler(mrg8g_server* sv) {
             }
             if (sl.tickets.empty()) break;
             sv->peak_bytes = std::max(sv->peak_bytes, sv->arena->used());
-            describe_slot(sv, sl, insts, tiles);
+            describe_slot(sv, sl, insts, base, &tile_elems);
             sl.busy = true;
             sv->launches++;
             sv->launched_requests += sl.tickets.size();
             lk.unlock();
-            const int rc = enqueue_slot(sv, sl, insts, tiles);
+            const int rc = enqueue_slot(sv, sl, insts, base, tile_elems);
             std::string msg = rc ? mrg8g_last_error() : "";
             lk.lock();
             if (rc) {
@@ -357,18 +396,18 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
         destroy_server(sv);
         return cuda_fail(e, "serving: arena allocation");
     }
-    // Tiles per launch are bounded by the arena: an instance has at most one
-    // head and one partial tile, and a full tile covers tile_rows rows of
-    // 32 * kBatchLayoutV elements of at least 4 bytes.
-    const size_t min_tile_bytes = (size_t)c.tile_rows * 32 * kBatchLayoutV * 4;
-    const size_t tiles_cap = c.budget_bytes / min_tile_bytes + 3 * (size_t)c.max_batch + 16;
+    // A launch's tile count (at most 2 per request plus its bytes / 4 KiB,
+    // 4 KiB being the shortest body tile) must fit the kernel's 32-bit queue.
+    if (c.budget_bytes / 4096 + 2ull * c.max_batch >= 0xFFFFFFFFull) {
+        destroy_server(sv);
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "budget or max_batch too large");
+    }
     sv->slots.resize(c.inflight);
     for (uint32_t i = 0; i < c.inflight; ++i) {
         Slot& sl = sv->slots[i];
         sl.idx = (int)i;
         sl.server = sv;
-        sl.tiles_cap = tiles_cap;
-        const size_t stage = c.max_batch * sizeof(BatchInst) + tiles_cap * sizeof(BatchTile);
+        const size_t stage = c.max_batch * sizeof(BatchInst) + ((size_t)c.max_batch + 1) * sizeof(uint32_t);
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaMalloc(&sl.d_stage, stage)) != cudaSuccess ||
             (e = cudaMalloc(&sl.d_counter, 2 * sizeof(uint32_t))) != cudaSuccess ||
