@@ -169,6 +169,10 @@ typedef struct mrg8g_batch_config {
     int32_t threads;       /* threads per block, 128 or 256 (128)            */
     int32_t blocks_per_sm; /* resident blocks per SM cap (0 = occupancy max) */
     int32_t use_graph;     /* 1: launch through a captured CUDA graph        */
+    int32_t tiling;        /* 0: the host lists every tile, longest first;
+                              1: the kernel derives the tiles from per-instance
+                              tile counts (instances longest first): host work
+                              and descriptor bytes O(instances), not O(tiles) */
 } mrg8g_batch_config;
 
 typedef struct mrg8g_batch mrg8g_batch;
@@ -212,8 +216,9 @@ MRG8G_API int mrg8g_generate_each(const mrg8g_instance *inst, uint64_t count, vo
  * race; calls on the same stream are ordered. */
 MRG8G_API int mrg8g_batch_generate_noalloc(const mrg8g_instance *inst, uint64_t count, void *stream);
 
-/* Time the candidate shapes on this batch (synchronises `stream`), keep the
- * fastest and report it in *chosen (may be NULL). */
+/* Time the candidate shapes on this batch (tile rows 128..2048 x 128 or 256
+ * threads x both tilings; synchronises `stream`), keep the fastest and report
+ * it in *chosen (may be NULL). */
 MRG8G_API int mrg8g_batch_autotune(mrg8g_batch *b, void *stream, mrg8g_batch_config *chosen);
 
 MRG8G_API int mrg8g_batch_get_config(const mrg8g_batch *b, mrg8g_batch_config *cfg);

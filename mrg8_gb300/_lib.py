@@ -134,7 +134,7 @@ class LoadtestResult(C.Structure):
 class BatchConfig(C.Structure):
     """mrg8g_batch_config of include/mrg8g.h."""
     _fields_ = [("tile_rows", C.c_int32), ("threads", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("use_graph", C.c_int32)]
+                ("use_graph", C.c_int32), ("tiling", C.c_int32)]
 
 
 class MRG8GError(RuntimeError):

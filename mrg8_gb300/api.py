@@ -289,7 +289,7 @@ class Batch:
     """
 
     def __init__(self, instances, tile_rows: int = 0, threads: int = 0, blocks_per_sm: int = 0,
-                 use_graph: bool = True):
+                 use_graph: bool = True, tiling: int = 0):
         self._lib = _lib.load()
         items = []
         self._keep = []
@@ -311,7 +311,7 @@ class Batch:
             self._keep.append(out)
         arr = (_lib.Instance * max(len(items), 1))(*items)
         self._arr, self._count = arr, len(items)
-        cfg = _lib.BatchConfig(tile_rows, threads, blocks_per_sm, 1 if use_graph else 0)
+        cfg = _lib.BatchConfig(tile_rows, threads, blocks_per_sm, 1 if use_graph else 0, tiling)
         self.device = device
         h = C.c_void_p()
         with torch.cuda.device(device or torch.cuda.current_device()):
@@ -337,14 +337,26 @@ class Batch:
             s = torch.cuda.current_stream().cuda_stream
             check(self._lib.mrg8g_batch_autotune(self._h, C.c_void_p(s), C.byref(cfg)))
         return {"tile_rows": cfg.tile_rows, "threads": cfg.threads, "blocks_per_sm": cfg.blocks_per_sm,
-                "use_graph": cfg.use_graph}
+                "use_graph": cfg.use_graph, "tiling": cfg.tiling}
 
     @property
     def config(self) -> dict:
         cfg = _lib.BatchConfig()
         check(self._lib.mrg8g_batch_get_config(self._h, C.byref(cfg)))
         return {"tile_rows": cfg.tile_rows, "threads": cfg.threads, "blocks_per_sm": cfg.blocks_per_sm,
-                "use_graph": cfg.use_graph}
+                "use_graph": cfg.use_graph, "tiling": cfg.tiling}
+
+    def set_config(self, **kw) -> dict:
+        """Change the launch shape (keys of ``config``; the others are kept)."""
+        cur = self.config
+        unknown = set(kw) - set(cur)
+        if unknown:
+            raise ValueError(f"unknown batch config keys {sorted(unknown)}")
+        cur.update(kw)
+        cfg = _lib.BatchConfig(cur["tile_rows"], cur["threads"], cur["blocks_per_sm"], 1 if cur["use_graph"] else 0,
+                               cur["tiling"])
+        check(self._lib.mrg8g_batch_set_config(self._h, C.byref(cfg)))
+        return self.config
 
     def stats(self) -> dict:
         t, o, b = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -39,6 +39,26 @@ void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vect
     });
 }
 
+void sort_largest_first(BatchInst* insts, uint32_t count) {
+    std::stable_sort(insts, insts + count, [](const BatchInst& x, const BatchInst& y) {
+        return x.n * kind_elem_bytes(x.kind) > y.n * kind_elem_bytes(y.kind);
+    });
+}
+
+uint64_t tile_prefix(const BatchInst* insts, uint32_t count, uint64_t tile_elems, uint32_t* base) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        base[i] = (uint32_t)total;
+        const BatchInst& d = insts[i];
+        if (!d.n) continue;
+        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
+        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
+        total += (head ? 1 : 0) + (d.n - head + tile_elems - 1) / tile_elems;
+    }
+    base[count] = (uint32_t)total;
+    return total;
+}
+
 }  // namespace mrg8g
 
 struct mrg8g_batch {
@@ -52,6 +72,10 @@ struct mrg8g_batch {
     BatchTile* d_tiles = nullptr;
     uint32_t* d_counter = nullptr;
     size_t d_tiles_cap = 0;
+    uint32_t* d_base = nullptr;    // tile prefix counts (derived tiling)
+    bool d_insts_sorted = false;   // d_insts holds the longest-first order
+    bool planned = false;
+    uint64_t ntiles = 0;
     cudaStream_t cap = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -73,6 +97,36 @@ int normalise(mrg8g_batch_config& c) {
     if (c.threads != 128 && c.threads != 256) return fail(MRG8G_ERR_INVALID_ARGUMENT, "threads must be 128 or 256");
     if (c.blocks_per_sm < 0) return fail(MRG8G_ERR_INVALID_ARGUMENT, "negative blocks_per_sm");
     if (c.use_graph < 0 || c.use_graph > 1) return fail(MRG8G_ERR_INVALID_ARGUMENT, "use_graph must be 0 or 1");
+    if (c.tiling < 0 || c.tiling > 1) return fail(MRG8G_ERR_INVALID_ARGUMENT, "tiling must be 0 or 1");
+    return MRG8G_SUCCESS;
+}
+
+int upload_insts(mrg8g_batch* b, const BatchInst* src, bool sorted) {
+    cudaError_t e;
+    if (!b->insts.empty() &&
+        (e = cudaMemcpy(b->d_insts, src, b->insts.size() * sizeof(BatchInst), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(instances)");
+    b->d_insts_sorted = sorted;
+    return MRG8G_SUCCESS;
+}
+
+// Derived tiling: instances longest first in d_insts, prefix counts in d_base.
+int plan_derived(mrg8g_batch* b) {
+    const uint32_t count = (uint32_t)b->insts.size();
+    std::vector<BatchInst> sorted(b->insts);
+    sort_largest_first(sorted.data(), count);
+    std::vector<uint32_t> base(count + 1);
+    const uint64_t total = tile_prefix(sorted.data(), count, (uint64_t)b->cfg.tile_rows * 32 * kBatchLayoutV, base.data());
+    if (total > 0xFFFFFFFFull) return fail(MRG8G_ERR_INVALID_ARGUMENT, "more than 2^32-1 tiles; raise tile_rows");
+    cudaError_t e;
+    if (!b->d_base && (e = cudaMalloc(&b->d_base, base.size() * sizeof(uint32_t))) != cudaSuccess)
+        return cuda_fail(e, "cudaMalloc(tile counts)");
+    if ((e = cudaMemcpy(b->d_base, base.data(), base.size() * sizeof(uint32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(tile counts)");
+    int rc = upload_insts(b, sorted.data(), true);
+    if (rc) return rc;
+    b->tiles.clear();
+    b->ntiles = total;
     return MRG8G_SUCCESS;
 }
 
@@ -100,18 +154,28 @@ int apply_config(mrg8g_batch* b, const mrg8g_batch_config& c) {
     mrg8g_batch_config n = c;
     int rc = normalise(n);
     if (rc) return rc;
-    const bool retile = n.tile_rows != b->cfg.tile_rows || b->tiles.empty();
+    const bool retile = n.tile_rows != b->cfg.tile_rows || n.tiling != b->cfg.tiling || !b->planned;
     b->cfg = n;
     if (retile) {
-        build_tiles(b);
-        if ((rc = upload_tiles(b))) return rc;
+        b->planned = false;
+        if (n.tiling) {
+            if ((rc = plan_derived(b))) return rc;
+        } else {
+            build_tiles(b);
+            if ((rc = upload_tiles(b))) return rc;
+            if (b->d_insts_sorted && (rc = upload_insts(b, b->insts.data(), false))) return rc;
+            if (b->tiles.size() > 0xFFFFFFFFull)
+                return fail(MRG8G_ERR_INVALID_ARGUMENT, "more than 2^32-1 tiles; raise tile_rows");
+            b->ntiles = b->tiles.size();
+        }
+        b->planned = true;
     }
     const int sms = device_sms();
     if (!sms) return MRG8G_ERR_CUDA;
     int bps = batch_blocks_per_sm(n.threads);
     if (n.blocks_per_sm > 0 && n.blocks_per_sm < bps) bps = n.blocks_per_sm;
     const uint64_t wpb = (uint64_t)n.threads / 32;
-    const uint64_t want = (b->tiles.size() + wpb - 1) / wpb;
+    const uint64_t want = (b->ntiles + wpb - 1) / wpb;
     b->blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * bps, want));
     release_graph(b);
     return MRG8G_SUCCESS;
@@ -120,13 +184,13 @@ int apply_config(mrg8g_batch* b, const mrg8g_batch_config& c) {
 BatchArgs args_of(const mrg8g_batch* b) {
     BatchArgs a;
     a.insts = b->d_insts;
-    a.tiles = b->d_tiles;
-    a.ntiles = (uint32_t)b->tiles.size();
+    a.tiles = b->cfg.tiling ? nullptr : b->d_tiles;
+    a.ntiles = (uint32_t)b->ntiles;
     a.counter = b->d_counter;
     a.done_blocks = nullptr;
-    a.tile_base = nullptr;
+    a.tile_base = b->cfg.tiling ? b->d_base : nullptr;
     a.ninst = (uint32_t)b->insts.size();
-    a.tile_elems = 0;
+    a.tile_elems = (uint32_t)((uint64_t)b->cfg.tile_rows * 32 * kBatchLayoutV);
     a.states = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     return a;
@@ -167,6 +231,7 @@ void destroy_plan(mrg8g_batch* b) {
     if (b->d_insts) cudaFree(b->d_insts);
     if (b->d_tiles) cudaFree(b->d_tiles);
     if (b->d_counter) cudaFree(b->d_counter);
+    if (b->d_base) cudaFree(b->d_base);
     delete b;
 }
 
@@ -241,7 +306,7 @@ int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_b
 
 int mrg8g_batch_launch(mrg8g_batch* b, void* stream) {
     if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
-    if (b->tiles.empty()) return MRG8G_SUCCESS;
+    if (!b->ntiles) return MRG8G_SUCCESS;
     cudaStream_t s = (cudaStream_t)stream;
     if (!b->cfg.use_graph) return enqueue(b, s);
     int rc;
@@ -264,7 +329,7 @@ int mrg8g_batch_set_config(mrg8g_batch* b, const mrg8g_batch_config* cfg) {
 
 int mrg8g_batch_stats(const mrg8g_batch* b, uint64_t* tiles, uint64_t* outputs, uint64_t* bytes) {
     if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
-    if (tiles) *tiles = b->tiles.size();
+    if (tiles) *tiles = b->ntiles;
     if (outputs) *outputs = b->outputs;
     if (bytes) *bytes = b->bytes;
     return MRG8G_SUCCESS;
@@ -272,7 +337,7 @@ int mrg8g_batch_stats(const mrg8g_batch* b, uint64_t* tiles, uint64_t* outputs, 
 
 int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chosen) {
     if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
-    if (b->tiles.empty()) {
+    if (!b->ntiles) {
         if (chosen) *chosen = b->cfg;
         return MRG8G_SUCCESS;
     }
@@ -289,7 +354,8 @@ int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chose
     int rc = MRG8G_SUCCESS;
     for (int r : rows) {
         for (int t : threads) {
-            mrg8g_batch_config c{r, t, 0, use_graph};
+          for (int tiling = 0; tiling < 2; ++tiling) {
+            mrg8g_batch_config c{r, t, 0, use_graph, tiling};
             if ((rc = apply_config(b, c))) break;
             if ((rc = mrg8g_batch_launch(b, s))) break;  // warm-up (and graph build)
             cudaEventRecord(e0, s);
@@ -302,6 +368,8 @@ int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chose
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             if (ms < best_ms) best_ms = ms, best = c;
+          }
+          if (rc) break;
         }
         if (rc) break;
     }

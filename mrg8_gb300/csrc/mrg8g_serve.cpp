@@ -183,25 +183,13 @@ void describe_slot(mrg8g_server* sv, Slot& sl, std::vector<BatchInst>& insts, st
         d.slot1 = q.r.generator == MRG8G_NO_GENERATOR ? 0u : q.r.generator + 1u;
         rows += (d.n + D - 1) / D;
     }
-    std::stable_sort(insts.begin(), insts.end(), [](const BatchInst& x, const BatchInst& y) {
-        return x.n * kind_elem_bytes(x.kind) > y.n * kind_elem_bytes(y.kind);
-    });
+    sort_largest_first(insts.data(), count);
     const uint64_t warps = launch_warps(sv);
     uint64_t tr = ((rows + warps - 1) / warps + 7) / 8 * 8;
     tr = std::min<uint64_t>(std::max<uint64_t>(tr, kMinServeTileRows), (uint64_t)sv->cfg.tile_rows);
-    const uint64_t T = tr * D;
-    *tile_elems = (uint32_t)T;
+    *tile_elems = (uint32_t)(tr * D);
     base.resize(count + 1);
-    uint64_t total = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-        base[i] = (uint32_t)total;
-        const BatchInst& d = insts[i];
-        if (!d.n) continue;
-        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
-        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
-        total += (head ? 1 : 0) + (d.n - head + T - 1) / T;
-    }
-    base[count] = (uint32_t)total;
+    tile_prefix(insts.data(), count, tr * D, base.data());  // < 2^32 (checked at creation)
 }
 
 // Enqueue slot `sl`'s batch on its stream (lock not held; the slot is owned

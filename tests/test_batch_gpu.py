@@ -112,6 +112,36 @@ def test_batch_relaunch_autotune_and_plain_launch_agree(cuda, oracle):
     check_canaries(meta)
 
 
+@pytest.mark.parametrize("tile_rows,threads", [(16, 128), (24, 256), (512, 128)])
+def test_device_derived_tiles_match_oracle(cuda, oracle, tile_rows, threads):
+    """Tiles derived by the kernel from per-instance tile counts (unaligned
+    heads, zero and tiny lengths, random offsets, more than 32 instances so
+    that the owner search takes two levels) give every instance its own
+    sequential stream, and switching a plan between the two tilings keeps
+    the values."""
+    import torch
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(77 + tile_rows)
+    insts, meta = make_instances(cuda, rng, 90, 16)
+    b = m.Batch(insts, tile_rows=tile_rows, threads=threads, tiling=1)
+    assert b.config["tiling"] == 1
+    b.launch()
+    torch.cuda.synchronize()
+    for (st, off, n, kind, buf, lead), (_, _, view, _) in zip(meta, insts):
+        want = expected(oracle, st, off, n, kind)
+        assert np.array_equal(as_bytes(view), want.view(np.uint8)), (off, n, kind, lead)
+    check_canaries(meta)
+    first = [as_bytes(v).copy() for (_, _, v, _) in insts]
+    for tiling in (0, 1):
+        assert b.set_config(tiling=tiling)["tiling"] == tiling
+        for (_, _, v, _) in insts:
+            v.zero_()
+        b.launch()
+        torch.cuda.synchronize()
+        assert all(np.array_equal(as_bytes(v), f) for (_, _, v, _), f in zip(insts, first)), tiling
+    check_canaries(meta)
+
+
 def test_uneven_batch_distribution_small(cuda, oracle):
     """The uneven-batch distribution at reduced scale: distinct seeds, lengths
     log-uniform in [1, 2^18], dtypes mixed uniformly; every instance equal to
