@@ -35,6 +35,7 @@
 #include "../../include/mrg8g.h"
 #include "mrg8g_internal.h"
 #include "mrg8g_runtime.h"
+#include "mrg8g_arena.h"
 #include "mrg8g_tables.h"
 
 using namespace mrg8g;
@@ -46,66 +47,11 @@ double now_s() {
     return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
-// First-in first-out arena over [0, cap): blocks are handed out in admission
-// order and reclaimed from the oldest once released (out-of-order releases
-// wait for the older ones).  256-byte granularity.
-class Arena {
-public:
-    explicit Arena(uint64_t cap) : cap_(cap) {}
-    bool alloc(uint64_t bytes, uint64_t* off) {
-        bytes = bytes ? (bytes + 255) / 256 * 256 : 256;
-        if (bytes > cap_) return false;
-        if (blocks_.empty()) head_ = tail_ = 0;
-        // Live blocks occupy [tail, head) or, once wrapped, [tail, cap) + [0, head).
-        const bool wrapped = !blocks_.empty() && head_ <= tail_;
-        uint64_t at;
-        if (!wrapped) {
-            if (cap_ - head_ >= bytes) {
-                at = head_;
-            } else if (tail_ >= bytes) {
-                if (head_ < cap_) blocks_.push_back({head_, cap_ - head_, true});  // unused end
-                at = 0;
-            } else {
-                return false;
-            }
-        } else if (tail_ - head_ >= bytes) {
-            at = head_;
-        } else {
-            return false;
-        }
-        blocks_.push_back({at, bytes, false});
-        head_ = at + bytes;
-        used_ += bytes;
-        *off = at;
-        return true;
-    }
-    void release(uint64_t off) {
-        for (auto& b : blocks_)
-            if (b.off == off && !b.released) {
-                b.released = true;
-                used_ -= b.size;
-                break;
-            }
-        while (!blocks_.empty() && blocks_.front().released) blocks_.pop_front();
-        if (blocks_.empty()) head_ = tail_ = 0;
-        else tail_ = blocks_.front().off;
-    }
-    uint64_t used() const { return used_; }
-
-private:
-    struct Block {
-        uint64_t off, size;
-        bool released;
-    };
-    uint64_t cap_, head_ = 0, tail_ = 0, used_ = 0;
-    std::deque<Block> blocks_;
-};
-
 struct Req {
     mrg8g_request r;
     uint32_t state[8];  // stateless requests
     uint64_t offset;    // jump distance from the (embedded or table) state
-    uint64_t bytes = 0, arena_off = 0;
+    uint64_t bytes = 0, arena_off = 0, arena_seq = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
     int status = MRG8G_SUCCESS;
     bool done = false;
@@ -132,7 +78,7 @@ struct mrg8g_server {
     uint32_t* d_states = nullptr;
     std::vector<uint64_t> gen_pos;
     std::vector<std::array<uint32_t, 8>> gen_state;
-    std::unique_ptr<Arena> arena;
+    std::unique_ptr<mrg8g::Arena> arena;
     std::vector<Slot> slots;
 
     std::mutex mu;
@@ -301,7 +247,7 @@ void scheduler(mrg8g_server* sv) {
             const double t = now_s();
             while (!sv->pending.empty() && sl.tickets.size() < sv->cfg.max_batch) {
                 Req& q = sv->reqs[sv->pending.front()];
-                if (!sv->arena->alloc(q.bytes, &q.arena_off)) break;  // head of line waits for space
+                if (!sv->arena->alloc(q.bytes, &q.arena_off, &q.arena_seq)) break;  // head of line waits for space
                 q.t_admit = t;
                 sl.tickets.push_back(sv->pending.front());
                 sv->pending.pop_front();
@@ -376,7 +322,7 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
     sv->dev = dev;
     sv->sms = device_sms();
     sv->bps = batch_blocks_per_sm(c.threads);
-    sv->arena.reset(new Arena(c.budget_bytes));
+    sv->arena.reset(new mrg8g::Arena(c.budget_bytes));
     sv->gen_pos.reserve(1024);
     cudaError_t e;
     if ((e = cudaMalloc(&sv->arena_base, c.budget_bytes)) != cudaSuccess ||
@@ -529,7 +475,7 @@ int mrg8g_server_release(mrg8g_server* sv, uint64_t ticket) {
     auto it = sv->reqs.find(ticket);
     if (it == sv->reqs.end()) return fail(MRG8G_ERR_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
     if (!it->second.done) return fail(MRG8G_ERR_NOT_READY, "ticket %llu is not complete", (unsigned long long)ticket);
-    if (it->second.t_admit > 0) sv->arena->release(it->second.arena_off);
+    if (it->second.t_admit > 0) sv->arena->release(it->second.arena_seq);
     sv->reqs.erase(it);
     sv->wake_seq.fetch_add(1, std::memory_order_release);
     sv->cv_sched.notify_one();

@@ -1,0 +1,69 @@
+// check_arena.cpp -- CPU property check of the serving output arena.
+//
+// Built by tests/test_arena.py with g++ against mrg8_gb300/csrc/mrg8g_arena.h.
+// Random admissions and out-of-order releases (a FIFO window of live requests
+// released in shuffled order, as completions and client releases interleave)
+// against an independent model: every block lies in [0, cap) on a 256-byte
+// boundary, no two live blocks overlap, used() is the sum of the live sizes,
+// an empty arena takes a request of any size up to cap, and releasing
+// everything returns the arena to empty.  Prints "ok <allocations>" on success.
+#include <algorithm>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+#include "mrg8g_arena.h"
+
+struct Live {
+    uint64_t seq, off, size;
+};
+
+static int fail(const char* what, unsigned long long a, unsigned long long b) {
+    std::printf("FAIL %s %llu %llu\n", what, a, b);
+    return 1;
+}
+
+int main() {
+    std::mt19937_64 rng(12345);
+    unsigned long long allocations = 0;
+    for (int round = 0; round < 40; ++round) {
+        const uint64_t cap = (uint64_t)(1 + rng() % 64) << (12 + round % 12);
+        mrg8g::Arena a(cap);
+        std::vector<Live> live;
+        uint64_t used = 0;
+        const int window = 1 + (int)(rng() % 200);
+        for (int step = 0; step < 20000; ++step) {
+            const bool do_alloc = live.size() < (size_t)window && (rng() % 3 != 0);
+            if (do_alloc) {
+                const uint64_t want = rng() % 5 == 0 ? 0 : 1 + rng() % std::max<uint64_t>(1, cap / (1 + rng() % 16));
+                uint64_t off = 0, seq = 0;
+                if (!a.alloc(want, &off, &seq)) {
+                    if (live.empty() && want <= cap) return fail("empty arena refused", want, cap);
+                    continue;
+                }
+                ++allocations;
+                const uint64_t size = want ? (want + 255) / 256 * 256 : 256;
+                if (off % 256 || off + size > cap) return fail("block outside the arena", off, size);
+                for (const Live& l : live)
+                    if (off < l.off + l.size && l.off < off + size) return fail("overlap", off, l.off);
+                live.push_back({seq, off, size});
+                used += size;
+            } else if (!live.empty()) {
+                // release one of the oldest few, so releases come out of order
+                const size_t k = rng() % std::min<size_t>(live.size(), 8);
+                a.release(live[k].seq);
+                a.release(live[k].seq);  // a second release is ignored
+                used -= live[k].size;
+                live.erase(live.begin() + (long)k);
+            }
+            if (a.used() != used) return fail("used", a.used(), used);
+        }
+        std::shuffle(live.begin(), live.end(), rng);
+        for (const Live& l : live) a.release(l.seq);
+        if (a.used() != 0) return fail("not empty after releasing all", a.used(), 0);
+        uint64_t off = 1, seq = 0;
+        if (!a.alloc(cap, &off, &seq) || off != 0) return fail("full-size request after emptying", off, cap);
+    }
+    std::printf("ok %llu\n", allocations);
+    return 0;
+}
