@@ -93,8 +93,8 @@ int kind_elem_bytes(int kind) { return (kind == MRG8G_F64_ORIGINAL || kind == MR
 bool kind_valid(int kind) { return kind >= MRG8G_U32 && kind <= MRG8G_F32_SHIFTED; }
 
 // Substreams per lane: one 16-byte vector of outputs per row.
-// Two substreams per lane for every kind: 56 registers and 24 KB of shared
-// memory per block (9 blocks per SM); four per lane need 80 registers.
+// Two substreams per lane for every kind (fp32 measured 843 Gsamples/s at
+// 2^30 with two, 833 with four; u32 within 1 %).
 int default_layout_V(int) { return 2; }
 
 // Process-wide launch-shape overrides (mrg8g_tune_plain).
@@ -147,7 +147,7 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
     const uint64_t max_warps = (uint64_t)dev->sms * bps * (kPlainThreads / 32);
     uint64_t tile = (body + max_warps - 1) / max_warps;
     tile = (tile + D - 1) / D * D;
-    tile = std::max<uint64_t>(tile, D * 16);  // a short call still spreads over many warps
+    tile = std::max<uint64_t>(tile, D * 64);
     uint64_t warps = body ? (body + tile - 1) / tile : 1;
     const uint64_t blocks = (warps + kPlainThreads / 32 - 1) / (kPlainThreads / 32);
 

@@ -23,13 +23,6 @@ template <int V, int KIND>
 __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__ PlainArgs a) {
     using T = typename OutOf<KIND>::T;
     __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
-    // The A^(2^i) table in shared memory: a warp's jump to its tile start
-    // then waits on shared memory instead of on one L2 round trip per step,
-    // which is most of a short tile's time.
-    __shared__ __align__(16) uint32_t sjump[kDevJump * 64];
-    for (int q = threadIdx.x; q < kDevJump * 16; q += kPlainThreads)
-        reinterpret_cast<uint4*>(sjump)[q] = reinterpret_cast<const uint4*>(g_jump)[q];
-    __syncthreads();
     T* const out = static_cast<T*>(a.out);
     const int lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -39,7 +32,7 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__
         uint32_t st[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) st[q] = a.st[q];
-        lane_sequential<KIND>(sjump, st, out, a.head);  // row 0 of A = coefficients
+        lane_sequential<KIND>(g_jump, st, out, a.head);  // row 0 of A = coefficients
     }
 
     const uint64_t B = a.head + warp * a.tile;
@@ -47,7 +40,7 @@ __global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__
     uint32_t s[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = a.st[q];
-    warp_jump(sjump, s, B);
+    warp_jump(g_jump, s, B);
     warp_generate<V, KIND>(g_win, s, out + B, min(a.tile, a.n - B), a.lc, scratch[threadIdx.x >> 5]);
 }
 
@@ -101,14 +94,10 @@ static cudaError_t launch_plain_t(const PlainArgs& a, int blocks, cudaStream_t s
     return cudaGetLastError();
 }
 
-// Called once per kernel and device before the first launch: shared memory
-// is preferred over L1 (the blocks hold the jump table).
 template <int V, int KIND>
 static int occupancy_t() {
     int nb = 0;
-    if (cudaFuncSetAttribute(k_plain<V, KIND>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_plain<V, KIND>, kPlainThreads, 0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_plain<V, KIND>, kPlainThreads, 0) != cudaSuccess)
         return 1;
     return nb > 0 ? nb : 1;
 }
