@@ -65,8 +65,87 @@ def profiled_traffic(name: str):
     return float(m.group(1)) if m else None
 
 
+def gpu_id(index: int) -> str:
+    """nvidia-smi / NVML identity of CUDA device `index` (its UUID), so that a
+    restricted CUDA_VISIBLE_DEVICES still samples the GPU under test."""
+    try:
+        import torch
+        u = str(torch.cuda.get_device_properties(index).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return str(index)
+
+
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read through NVML (read-only queries)
+    every millisecond on a background thread, so that even a timed region of a
+    few tens of milliseconds holds many samples.  Falls back to nothing when
+    the NVML library cannot be loaded."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int, period_s: float = 1e-3):
+        import ctypes as C
+        self.C = C
+        self.period = period_s
+        self.samples = []
+        self.ok = False
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = C.c_void_p()
+            ident = gpu_id(index)
+            rc = (lib.nvmlDeviceGetHandleByUUID(ident.encode(), C.byref(h)) if ident.startswith("GPU-")
+                  else lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(int(ident)), C.byref(h)))
+            if rc != 0:
+                return
+            mx = C.c_uint()
+            self.max_mhz = float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0 else None
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.lib, self.h, self.ident = lib, h, ident
+            self.ok = True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _run(self):
+        C = self.C
+        clk, rs = C.c_uint(), C.c_ulonglong()
+        while not self.stop:
+            a = self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk))
+            b = self.reasons_fn(self.h, C.byref(rs))
+            if a == 0:
+                self.samples.append((float(clk.value), int(rs.value) if b == 0 else 0))
+            time.sleep(self.period)
+
+    def __enter__(self):
+        import threading
+        self.stop = False
+        if self.ok:
+            self.thread = threading.Thread(target=self._run, daemon=True)
+            self.thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop = True
+        if self.ok:
+            self.thread.join()
+
+    def summary(self):
+        if not self.ok or not self.samples:
+            return None
+        sm = [c for c, _ in self.samples]
+        reasons = sorted({name for _, r in self.samples for bit, name in self.REASONS.items() if r & bit})
+        loaded = [v for v in sm if self.max_mhz and v > 0.5 * self.max_mhz] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(sm), "source": "nvml, 1 ms", "gpu": self.ident}
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """Clocks and throttle reasons during the timed region: NVML every
+    millisecond where it loads, else nvidia-smi every 200 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -76,18 +155,24 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.tmp = None
+        self.nvml = NvmlClockSampler(index)
 
     def __enter__(self):
+        if self.nvml.ok:
+            self.nvml.__enter__()
+            return self
         try:
             self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                ["nvidia-smi", f"--id={gpu_id(self.index)}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
         return self
 
     def __exit__(self, *exc):
+        if self.nvml.ok:
+            self.nvml.__exit__(*exc)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -96,8 +181,12 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml.ok:
+            got = self.nvml.summary()
+            if got:
+                return got
         if self.proc is None or self.tmp is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no clock samples"]}
         self.tmp.flush()
         rows = []
         with open(self.tmp.name) as f:
