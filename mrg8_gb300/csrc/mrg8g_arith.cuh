@@ -57,31 +57,46 @@ MRG8G_HD uint32_t shl_clamp(uint32_t a, uint32_t s) {
 #endif
 }
 
-// IEEE-754 bits of RN(v * rnorm) for 0 <= v <= 2^31 - 1 (v = 0 gives +0).
-// With lz = clz(v) and xn = v << lz (leading one at bit 31), the exact
-// product scaled to [2^52, 2^53) is xn (2^31 + 1) / 2^10, so one multiply-add
-// forms it together with the round-to-nearest-even bias 0x1FF + bit 10 of xn;
-// its high word >> 10 plus the exponent field gives the high word of the
-// result (at most 0x3FF00000).  P_hi >= 2^30 for v >= 1 and P_hi = 0 for
-// v = 0, so min(high word, P_hi) maps v = 0 to +0 and changes nothing else.
-MRG8G_HD uint64_t f64_bits_of(uint32_t v) {
+// IEEE-754 bits of RN(v * rnorm), rnorm = 2^-31 + 2^-62 = RN(1/(2^31-1)).
+// The exact product is (v 2^31 + v) 2^-62.  With lz = clz(v) and
+// xm = (v << lz) >> 1 (leading one at bit 30), the 53-bit significand is
+// M = xm 2^22 + RNE(xm / 2^9), RNE(xm / 2^9) = (xm + 0xFF + bit 9 of xm) >> 9
+// (no overflow: xm < 2^31), and the biased exponent is 1023 - lz, entering
+// the high word as (1022 - lz) 2^20 plus M's leading one at bit 52.  The low
+// word (xm << 22) + RNE(...) carries into the high word only at v = p, whose
+// value rounds up to 1.0.  v = 0 gives xm = 0 and min(high word, xm) = 0
+// (xm >= 2^30 exceeds every high word otherwise).  Shifts and adds only: no
+// multiply, which would occupy the FMA-heavy pipe that the recurrence's
+// multiply-adds already saturate.
+//
+// For 0 <= v <= p - 1 (SHIFTED: v = S - 1).
+MRG8G_HD uint64_t f64_bits_below_p(uint32_t v) {
     const uint32_t lz = clz32(v);
-    const uint32_t xn = shl_clamp(v, lz);
-    const uint32_t bias = 0x1FFu + ((xn >> 10) & 1u);
-    const uint64_t P = mad_wide_u32(xn, 0x80000001u, bias);
-    const uint32_t phi = (uint32_t)(P >> 32);
-    const uint32_t lo = (uint32_t)(P >> 10);
-    uint32_t hi = (phi >> 10) + ((1022u - lz) << 20);
-    hi = hi < phi ? hi : phi;
+    const uint32_t xm = shl_clamp(v, lz) >> 1;
+    const uint32_t t = (xm + 0xFFu + ((xm >> 9) & 1u)) >> 9;
+    const uint32_t lo = (xm << 22) + t;
+    uint32_t hi = (xm >> 10) - (lz << 20) + (1022u << 20);
+    hi = hi < xm ? hi : xm;
+    return ((uint64_t)hi << 32) | lo;
+}
+
+// For 0 <= v <= p (ORIGINAL: v = S), with the low word's carry.
+MRG8G_HD uint64_t f64_bits_to_p(uint32_t v) {
+    const uint32_t lz = clz32(v);
+    const uint32_t xm = shl_clamp(v, lz) >> 1;
+    const uint32_t t = (xm + 0xFFu + ((xm >> 9) & 1u)) >> 9;
+    const uint32_t lo = (xm << 22) + t;
+    uint32_t hi = (xm >> 10) - (lz << 20) + (1022u << 20) + (lo < t ? 1u : 0u);
+    hi = hi < xm ? hi : xm;
     return ((uint64_t)hi << 32) | lo;
 }
 
 // IEEE-754 bits of (float)RN(v * rnorm) for 0 <= v <= 2^31 - 1.  A single
 // round-to-nearest-even of the exact product to 24 bits is
-// ((xn >> 1) + 0x40) >> 7 (xn is even and the halfway case cannot occur);
-// it equals the double rounding through fp64 for every v except
-// v = 0x7FFFFFBF, where the fp64 value lands on a halfway point and rounds up
-// once more.  v = 0 gives +0 through min(., xn).
+// ((xn >> 1) + 0x40) >> 7 with xn = v << lz (xn is even and the halfway case
+// cannot occur); it equals the double rounding through fp64 for every v
+// except v = 0x7FFFFFBF, where the fp64 value lands on a halfway point and
+// rounds up once more.  v = 0 gives +0 through min(., xn).
 MRG8G_HD uint32_t f32_bits_of(uint32_t v) {
     const uint32_t lz = clz32(v);
     const uint32_t xn = shl_clamp(v, lz);
@@ -91,8 +106,9 @@ MRG8G_HD uint32_t f32_bits_of(uint32_t v) {
 }
 
 // x is the stream value minus one, 0 <= x <= p - 1 (S = x + 1 in [1, p]).
-MRG8G_HD uint64_t f64_bits(uint32_t x, bool shifted) { return f64_bits_of(shifted ? x : x + 1u); }
+MRG8G_HD uint64_t f64_bits(uint32_t x, bool shifted) { return shifted ? f64_bits_below_p(x) : f64_bits_to_p(x + 1u); }
 MRG8G_HD uint32_t f32_bits(uint32_t x, bool shifted) { return f32_bits_of(shifted ? x : x + 1u); }
+
 
 // ------------------------------------------------------------ modular math
 

@@ -32,7 +32,7 @@ static int conv() {
         const float f = (float)d;
         uint32_t fb;
         std::memcpy(&fb, &f, 4);
-        if (db != f64_bits_of((uint32_t)v) || fb != f32_bits_of((uint32_t)v)) {
+        if (db != f64_bits_to_p((uint32_t)v) || fb != f32_bits_of((uint32_t)v)) {
             if (bad++ < 8) std::fprintf(stderr, "mismatch at v=%lu\n", (unsigned long)v);
         }
         // SHIFTED converts x = S - 1 = v; ORIGINAL converts v = x + 1.
