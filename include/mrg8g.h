@@ -245,7 +245,11 @@ typedef struct mrg8g_server_config {
                                 launch too small to fill the GPU with such
                                 tiles uses shorter ones (16 rows at least)  */
     int32_t threads;         /* batch-kernel block size, 128 or 256 (0: 128) */
-    int32_t reserved;        /* 0                                            */
+    int32_t spin_us;         /* the scheduler thread stays awake (one busy
+                                host core) this long after its last
+                                activity: 0 = 2000 us, < 0 = sleep as soon as
+                                nothing is in flight (lower CPU use, higher
+                                latency for the next request)               */
 } mrg8g_server_config;
 
 #define MRG8G_NO_GENERATOR 0xFFFFFFFFu

@@ -89,7 +89,7 @@ class ServerConfig(C.Structure):
     """mrg8g_server_config of include/mrg8g.h."""
     _fields_ = [("budget_bytes", C.c_uint64), ("max_batch", C.c_uint32), ("inflight", C.c_uint32),
                 ("max_generators", C.c_uint32), ("tile_rows", C.c_int32), ("threads", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("spin_us", C.c_int32)]
 
 
 NO_GENERATOR = 0xFFFFFFFF

@@ -189,9 +189,8 @@ void finish_slot(mrg8g_server* sv, Slot& sl, double t, int rc) {
 }
 
 // The scheduler spins (yielding) while launches are in flight and for
-// kSpinIdle seconds after the last activity, so that requests arriving at a
-// steady rate find it awake; after that it sleeps on cv_sched.
-constexpr double kSpinIdle = 2e-3;
+// cfg.spin_us after the last activity, so that requests arriving at a steady
+// rate find it awake; after that it sleeps on cv_sched.
 
 void scheduler(mrg8g_server* sv) {
     cudaSetDevice(sv->dev);
@@ -206,6 +205,7 @@ void scheduler(mrg8g_server* sv) {
     std::vector<Done> done;
     uint64_t seen = ~0ull;
     double active = now_s();
+    const double spin_idle = sv->cfg.spin_us < 0 ? 0.0 : sv->cfg.spin_us * 1e-6;
     bool inflight = false;
     while (!sv->stop.load(std::memory_order_acquire)) {
         // In-flight launches, polled without the lock (the scheduler thread
@@ -218,7 +218,7 @@ void scheduler(mrg8g_server* sv) {
         }
         const uint64_t ws = sv->wake_seq.load(std::memory_order_acquire);
         if (done.empty() && ws == seen) {  // nothing new
-            if (inflight || now_s() - active < kSpinIdle) {
+            if (inflight || now_s() - active < spin_idle) {
                 std::this_thread::yield();
                 continue;
             }
@@ -310,6 +310,7 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
     if (!c.max_generators) c.max_generators = 65536;
     if (!c.tile_rows) c.tile_rows = 256;
     if (!c.threads) c.threads = 128;
+    if (!c.spin_us) c.spin_us = 2000;
     if (c.tile_rows < 8 || (c.tile_rows & 7) || c.tile_rows > (1 << 16) || (c.threads != 128 && c.threads != 256) ||
         c.inflight > 16)
         return fail(MRG8G_ERR_INVALID_ARGUMENT, "bad server configuration");

@@ -19,9 +19,9 @@ class Server:
     batch kernel on ``inflight`` streams."""
 
     def __init__(self, budget_bytes: int = 16 << 30, max_batch: int = 1024, inflight: int = 3,
-                 max_generators: int = 65536, tile_rows: int = 0, threads: int = 0):
+                 max_generators: int = 65536, tile_rows: int = 0, threads: int = 0, spin_us: int = 0):
         self._lib = _lib.load()
-        cfg = _lib.ServerConfig(budget_bytes, max_batch, inflight, max_generators, tile_rows, threads, 0)
+        cfg = _lib.ServerConfig(budget_bytes, max_batch, inflight, max_generators, tile_rows, threads, spin_us)
         h = C.c_void_p()
         check(self._lib.mrg8g_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -166,3 +166,21 @@ def test_request_errors_are_reported(cuda):
         with pytest.raises(MRG8GError):
             srv.release(t)                             # released twice
         assert srv.stats()["error"] == 0
+
+
+def test_sleeping_scheduler_gives_the_same_results(cuda, oracle):
+    """spin_us < 0: the scheduler sleeps whenever nothing is in flight; requests
+    spaced out in time still complete with their own stream segments."""
+    from mrg8_gb300.serve import Server
+    rng = np.random.default_rng(11)
+    with Server(budget_bytes=64 << 20, spin_us=-1) as srv:
+        for j in range(12):
+            kind = KINDS[j % 5]
+            n = int(2 ** rng.uniform(4, 14))
+            seed = int(rng.integers(0, 2**32))
+            off = int(rng.integers(0, 2**40))
+            t = srv.submit(n, kind, seed=seed, offset=off, tag=j)
+            res = {}
+            drain(srv, 1, res)
+            assert np.array_equal(res[t][1].view(np.uint8), segment(oracle, seed, off, n, kind).view(np.uint8))
+            time.sleep(0.004)  # longer than any spin window: the next submit wakes a sleeping thread
