@@ -99,6 +99,31 @@ def test_sizes_and_alignment(cuda, oracle, kind):
         assert np.array_equal(g.get_state(), end), (n, kind)
 
 
+@pytest.mark.parametrize("V", [1, 2, 4])
+@pytest.mark.parametrize("kind", KINDS)
+def test_every_lane_layout(cuda, oracle, kind, V):
+    """Every lane layout the autotuner may pick (V substreams per lane, and a
+    cap on resident blocks) gives the same stream, at unaligned starts and at
+    sizes around the row and tile boundaries of that layout."""
+    import mrg8_gb300 as m
+    from mrg8_gb300 import _lib
+    lib = _lib.load()
+    try:
+        for bps in (0, 2):
+            _lib.check(lib.mrg8g_tune_plain(kind, V, bps))
+            g = m.MRG8(77 + 10 * V + kind)
+            rng = np.random.default_rng(V * 10 + kind + bps)
+            for n in (1, 3, 31 * V + 1, 32 * V * 8 + 5, 32 * V * 64 + 7, 1 << 20, 3_000_017):
+                offset = int(rng.integers(0, 4))
+                st = g.get_state()
+                ref, end = oracle.generate(st, n, kind, nthreads=4)
+                out = gen_device(g, n, kind, cuda, offset=offset)
+                assert np.array_equal(as_bytes(out), as_bytes(ref)), (V, bps, n, offset)
+                assert np.array_equal(g.get_state(), end)
+    finally:
+        _lib.check(lib.mrg8g_tune_plain(kind, 0, 0))
+
+
 @pytest.mark.parametrize("kind", [po.U32, po.F64_SHIFTED, po.F32_ORIGINAL])
 def test_consecutive_calls_continue_the_stream(cuda, oracle, kind):
     import mrg8_gb300 as m
