@@ -83,13 +83,23 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uin
     for (int q = 0; q < 8; ++q) s[q] = __shfl_sync(kFull, val, q << 2);
 }
 
-// Initial window of a lane for layout V: x[v][j] = S[B + V lane + v + d j] - 1
+// Initial window of a lane for layout V: x[v][j] = S[B + o + d j] - 1 with
+// o = sub_offset(lane, v) (V lane + v for the usual layouts)
 // for j = 0..7 (d = 32 V), from the state s taken at stream position B.  The
 // 8 V dot products run four at a time (the four table rows are loaded
 // together, so their latencies overlap, and the setup's register peak stays
 // below the main loop's) through the warp's scratch rows in shared memory,
 // `scratch` holding 8 V * 32 words laid out [slot][lane].
-template <int V>
+// Offset within a warp row (32 V outputs) of lane `lane`'s substream v, for
+// outputs of ELEM bytes.  A lane owns V consecutive outputs, except 8-byte
+// outputs with V = 4: there lane l owns the pairs at 2 l and 64 + 2 l, so that
+// each 16-byte store instruction of the warp covers 512 contiguous bytes.
+template <int V, int ELEM>
+MRG8G_HDC uint32_t sub_offset(uint32_t lane, uint32_t v) {
+    return (ELEM == 8 && V == 4) ? 64u * (v >> 1) + 2u * lane + (v & 1u) : (uint32_t)V * lane + v;
+}
+
+template <int V, int ELEM>
 __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t s[8],
                                             int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
     const uint32_t* w = win + win_offset(layout_index(V));
@@ -99,7 +109,7 @@ __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, co
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int i = i0 + q, v = i >> 3, j = i & 7;
-            const uint4* row = reinterpret_cast<const uint4*>(w + ((V * lane + v) * 8 + j) * 8);
+            const uint4* row = reinterpret_cast<const uint4*>(w + (sub_offset<V, ELEM>(lane, v) * 8 + j) * 8);
             r[2 * q] = __ldg(row);
             r[2 * q + 1] = __ldg(row + 1);
         }

@@ -26,7 +26,8 @@ __device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapC
     }
 }
 
-// Store slot u of every substream of the lane as V consecutive elements at p.
+// Store slot u of every substream of the lane at p, the lane's first output
+// of the row (the others follow sub_offset).
 template <int V, int KIND>
 __device__ __forceinline__ void store_vec(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u) {
     using T = typename OutOf<KIND>::T;
@@ -34,9 +35,10 @@ __device__ __forceinline__ void store_vec(typename OutOf<KIND>::T* p, const uint
         if constexpr (V == 1) {
             p[0] = convert<KIND>(x[0][u]);
         } else {
+            // pairs at p + 64 h / 2 (sub_offset: each store covers 512 contiguous bytes)
 #pragma unroll
             for (int h = 0; h < V; h += 2)
-                *reinterpret_cast<ulonglong2*>(p + h) =
+                *reinterpret_cast<ulonglong2*>(p + 32 * h) =
                     make_ulonglong2(convert<KIND>(x[h][u]), convert<KIND>(x[h + 1][u]));
         }
     } else {
@@ -54,14 +56,18 @@ __device__ __forceinline__ void store_vec(typename OutOf<KIND>::T* p, const uint
 // Row `row` of the run, checked element by element against its length.
 template <int V, int KIND>
 __device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const uint32_t (&x)[V][8], int u,
-                                              uint64_t row, uint64_t full, uint64_t len, uint32_t lane_off) {
+                                              uint64_t row, uint64_t full, uint64_t len, uint32_t lane) {
+    using T = typename OutOf<KIND>::T;
     constexpr uint32_t D = 32 * V;
     if (row < full) {
         store_vec<V, KIND>(p + row * D, x, u);
     } else {
+        const uint32_t base = sub_offset<V, sizeof(T)>(lane, 0);
 #pragma unroll
-        for (int v = 0; v < V; ++v)
-            if (row * D + lane_off + v < len) p[row * D + v] = convert<KIND>(x[v][u]);
+        for (int v = 0; v < V; ++v) {
+            const uint32_t o = sub_offset<V, sizeof(T)>(lane, v);
+            if (row * D + o < len) p[row * D + (o - base)] = convert<KIND>(x[v][u]);
+        }
     }
 }
 
@@ -75,15 +81,14 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
     constexpr uint32_t D = 32 * V;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
-    lane_window<V>(win, s, lane, scratch, x);
+    lane_window<V, sizeof(T)>(win, s, lane, scratch, x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
-    const uint32_t lane_off = (uint32_t)V * (uint32_t)lane;
-    T* const p = out + lane_off;
+    T* const p = out + sub_offset<V, sizeof(T)>((uint32_t)lane, 0);
 
 #pragma unroll
     for (int u = 0; u < 8; ++u)
-        if ((uint64_t)u < rows) store_checked<V, KIND>(p, x, u, (uint64_t)u, full, len, lane_off);
+        if ((uint64_t)u < rows) store_checked<V, KIND>(p, x, u, (uint64_t)u, full, len, (uint32_t)lane);
 
     uint64_t m = 8;
     for (; m + 8 <= full; m += 8) {
@@ -97,7 +102,7 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
             leap_row<V>(x, u, lc);
-            if (m + u < rows) store_checked<V, KIND>(p, x, u, m + u, full, len, lane_off);
+            if (m + u < rows) store_checked<V, KIND>(p, x, u, m + u, full, len, (uint32_t)lane);
         }
     }
 }
