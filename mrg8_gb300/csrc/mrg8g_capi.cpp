@@ -93,9 +93,10 @@ int kind_elem_bytes(int kind) { return (kind == MRG8G_F64_ORIGINAL || kind == MR
 bool kind_valid(int kind) { return kind >= MRG8G_U32 && kind <= MRG8G_F32_SHIFTED; }
 
 // Substreams per lane: one 16-byte vector of outputs per row.
-// Two substreams per lane for every kind (fp32 measured 843 Gsamples/s at
-// 2^30 with two, 833 with four; u32 within 1 %).
-int default_layout_V(int) { return 2; }
+// Substreams per lane: two for 8-byte outputs (776 Gsamples/s fp64 SHIFTED at
+// 2^30, against 756 with four), four for 4-byte outputs (fp32 834 vs 829,
+// u32 1003 vs 993).
+int default_layout_V(int kind) { return kind_elem_bytes(kind) == 8 ? 2 : 4; }
 
 // Process-wide launch-shape overrides (mrg8g_tune_plain).
 static std::atomic<int> g_tune_V[5];
