@@ -148,7 +148,7 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
     const uint64_t max_warps = (uint64_t)dev->sms * bps * (kPlainThreads / 32);
     uint64_t tile = (body + max_warps - 1) / max_warps;
     tile = (tile + D - 1) / D * D;
-    tile = std::max<uint64_t>(tile, D * 64);
+    tile = std::max<uint64_t>(tile, std::max<uint64_t>(D * 32, 4096));  // >= 4096 outputs and 32 rows per warp
     uint64_t warps = body ? (body + tile - 1) / tile : 1;
     const uint64_t blocks = (warps + kPlainThreads / 32 - 1) / (kPlainThreads / 32);
 
