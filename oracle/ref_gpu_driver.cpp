@@ -17,12 +17,15 @@
  * (cuda/mrg8_cuda.cu:414-425): TNUM / BS blocks of BS threads,
  * each_itr = n / (TNUM / 32).
  *
- *   ref_gpu_driver <cubin> check <n> <seed> <TNUM> <BS> <out.bin>
+ *   ref_gpu_driver <cubin> check <n> <seed> <TNUM> <BS> <out.bin> [inner]
  *       one launch; writes the n fp64 outputs and then the 8-word next state
  *       (newest first) to out.bin
- *   ref_gpu_driver <cubin> time <n> <seed> <TNUM> <BS> <reps>
+ *   ref_gpu_driver <cubin> time <n> <seed> <TNUM> <BS> <reps> [inner]
  *       prints "TNUM BS n ms_per_launch Gsamples/s" (kernel time only, CUDA
  *       events around the launches)
+ * With "inner" the kernel is rng_inner (cuda/mrg8_cuda.cu:201-280), launched
+ * as mrg8_cuda::mrg8_inner does (cuda/mrg8_cuda.cu:402-412): TNUM / 64 blocks
+ * of 64 threads, each_itr = n / (TNUM / 64); BS is ignored.
  */
 #include <cuda.h>
 
@@ -51,10 +54,11 @@ int main(int argc, char** argv) {
         return 1;
     }
     const std::string mode = argv[2];
+    const bool inner = argc > 8 && std::string(argv[8]) == "inner";
     const int n = std::atoi(argv[3]);
     const uint32_t seed = (uint32_t)std::strtoul(argv[4], nullptr, 10);
     const int TNUM = std::atoi(argv[5]), BS = std::atoi(argv[6]);
-    if (n <= 0 || TNUM < 32 || BS < 32 || BS > 1024 || BS > TNUM || TNUM % BS || BS % 32) {
+    if (n <= 0 || TNUM < 64 || BS < 32 || BS > 1024 || BS > TNUM || TNUM % BS || BS % 32) {
         std::fprintf(stderr, "bad arguments\n");
         return 1;
     }
@@ -93,10 +97,10 @@ int main(int argc, char** argv) {
     for (CUfunction f : fs) {
         const char* name = nullptr;
         CK(cuFuncGetName(&name, f));
-        if (name && std::strstr(name, "rng_outer_32")) fn = f;
+        if (name && std::strstr(name, inner ? "rng_inner" : "rng_outer_32")) fn = f;
     }
     if (!fn) {
-        std::fprintf(stderr, "rng_outer_32 not found in %s\n", argv[1]);
+        std::fprintf(stderr, "%s not found in %s\n", inner ? "rng_inner" : "rng_outer_32", argv[1]);
         return 3;
     }
 
@@ -110,14 +114,17 @@ int main(int argc, char** argv) {
     CK(cuMemcpyHtoD(d_s32, s32.data(), s32.size() * 4));
     CK(cuMemcpyHtoD(d_state, rst, 32));
 
-    const int pnum = TNUM / 32;
+    const int pnum = inner ? TNUM / 64 : TNUM / 32;
     int each_itr = n / pnum;
-    const unsigned grid = (unsigned)(pnum / (BS / 32));
+    const unsigned grid = inner ? (unsigned)pnum : (unsigned)(pnum / (BS / 32));
+    const unsigned block = inner ? 64u : (unsigned)BS;
     uint64_t MASK = 2147483647ull;
     double rnorm = 1.0 / 2147483647.0;
     int nn = n;
-    void* args[] = {&d_ran, &d_jm, &d_s32, &d_state, &d_next, &nn, &MASK, &rnorm, &each_itr};
-    auto launch = [&] { CK(cuLaunchKernel(fn, grid, 1, 1, (unsigned)BS, 1, 1, 0, nullptr, args, nullptr)); };
+    void* args_outer[] = {&d_ran, &d_jm, &d_s32, &d_state, &d_next, &nn, &MASK, &rnorm, &each_itr};
+    void* args_inner[] = {&d_ran, &d_jm, &d_state, &d_next, &nn, &MASK, &rnorm, &each_itr};
+    void** args = inner ? args_inner : args_outer;
+    auto launch = [&] { CK(cuLaunchKernel(fn, grid, 1, 1, block, 1, 1, 0, nullptr, args, nullptr)); };
 
     if (mode == "check") {
         launch();

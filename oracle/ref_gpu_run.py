@@ -7,7 +7,8 @@ loader (`make -C oracle refgpu`).  Prints one JSON line:
 
     python oracle/ref_gpu_run.py [--n-check 2^24] [--n 2^30] [--reps 10]
 
-`check`: the kernel's outputs for seed 13579 at the reference's default launch
+`check`: the kernel's outputs (rng_outer_32, and rng_inner of
+cuda/mrg8_cuda.cu:201-280) for seed 13579 at the reference's default launch
 shape (65,536 threads in blocks of 64) against the oracle's SHIFTED fp64
 stream, bit for bit, and its next state.  `time`: the kernel alone (CUDA
 events around the launches, no allocation or copy of the reference's host
@@ -39,26 +40,27 @@ def build_driver() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "refgpu"], check=True)
 
 
-def check(n: int, tnum: int = 64 * 1024, bs: int = 64) -> dict:
+def check(n: int, tnum: int = 64 * 1024, bs: int = 64, kernel: str = "outer") -> dict:
     sys.path.insert(0, os.path.dirname(HERE))
     from oracle.pyoracle import F64_SHIFTED, Oracle
     o = Oracle()
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "out.bin")
-        subprocess.run([DRIVER, CUBIN, "check", str(n), str(SEED), str(tnum), str(bs), path], check=True)
+        subprocess.run([DRIVER, CUBIN, "check", str(n), str(SEED), str(tnum), str(bs), path, kernel], check=True)
         raw = np.fromfile(path, dtype=np.uint8)
     got = raw[: 8 * n].view(np.float64)
     nxt = raw[8 * n:].view(np.uint32)
     st = o.seed(SEED)
     want, end = o.generate(st, n, F64_SHIFTED, nthreads=os.cpu_count() or 4)
     diff = int(np.count_nonzero(got.view(np.uint64) != want.view(np.uint64)))
-    return {"n": n, "tnum": tnum, "bs": bs, "mismatches": diff, "next_state_equal": bool(np.array_equal(nxt, end))}
+    return {"kernel": kernel, "n": n, "tnum": tnum, "bs": bs, "mismatches": diff,
+            "next_state_equal": bool(np.array_equal(nxt, end))}
 
 
-def time_shapes(n: int, reps: int, shapes) -> list:
+def time_shapes(n: int, reps: int, shapes, kernel: str = "outer") -> list:
     rows = []
     for tnum, bs in shapes:
-        r = subprocess.run([DRIVER, CUBIN, "time", str(n), str(SEED), str(tnum), str(bs), str(reps)],
+        r = subprocess.run([DRIVER, CUBIN, "time", str(n), str(SEED), str(tnum), str(bs), str(reps), kernel],
                            capture_output=True, text=True, check=True)
         t, b, nn, ms, gs = r.stdout.split()
         rows.append({"tnum": int(t), "bs": int(b), "ms": float(ms), "gsamples_per_s": float(gs)})
@@ -80,8 +82,11 @@ def main() -> int:
     rows = time_shapes(args.n, args.reps, shapes)
     best = max(rows, key=lambda r: r["gsamples_per_s"])
     default = next(r for r in rows if r["tnum"] == 64 * 1024 and r["bs"] == 64)
+    chk_in = check(args.n_check, kernel="inner")
+    rows_in = time_shapes(args.n, max(1, args.reps // 5), [(t, 64) for t in (64 * 1024, 1024 * 1024)], "inner")
     print(json.dumps({"reference_gpu": "rng_outer_32", "check": chk, "n": args.n, "default_shape": default,
-                      "best_shape": best, "all": rows}))
+                      "best_shape": best, "all": rows,
+                      "rng_inner": {"check": chk_in, "shapes": rows_in}}))
     return 0
 
 
