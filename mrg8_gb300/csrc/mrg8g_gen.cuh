@@ -15,14 +15,15 @@ namespace mrg8g {
 
 // One row of every substream of the lane.  The oldest lag is accumulated
 // first so that only the last multiply-add waits for the previous row.
-template <int V>
+// ALU_TAIL selects reduce_acc_alu (4-byte outputs) over reduce_acc.
+template <int V, bool ALU_TAIL>
 __device__ __forceinline__ void leap_row(uint32_t (&x)[V][8], int u, const LeapCoef& lc) {
 #pragma unroll
     for (int v = 0; v < V; ++v) {
         uint64_t acc = lc.K1;
 #pragma unroll
         for (int k = 8; k >= 1; --k) acc = mad_wide_s32(lc.c[k - 1], x[v][(u - k) & 7], acc);
-        x[v][u] = reduce_acc(acc);
+        x[v][u] = ALU_TAIL ? reduce_acc_alu(acc) : reduce_acc(acc);
     }
 }
 
@@ -79,6 +80,7 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
                                               uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     constexpr uint32_t D = 32 * V;
+    constexpr bool kAluTail = sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
     lane_window<V, sizeof(T)>(win, s, lane, scratch, x);
@@ -94,14 +96,14 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
     for (; m + 8 <= full; m += 8) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            leap_row<V>(x, u, lc);
+            leap_row<V, kAluTail>(x, u, lc);
             store_vec<V, KIND>(p + (m + u) * D, x, u);
         }
     }
     if (m < rows) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            leap_row<V>(x, u, lc);
+            leap_row<V, kAluTail>(x, u, lc);
             if (m + u < rows) store_checked<V, KIND>(p, x, u, m + u, full, len, (uint32_t)lane);
         }
     }

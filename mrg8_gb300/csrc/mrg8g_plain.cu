@@ -19,8 +19,18 @@ namespace mrg8g {
 
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_plain)
 
+// Resident blocks the register allocation must allow: ten for fp64 with two
+// substreams per lane (48 registers), eight for 4-byte outputs with four.
 template <int V, int KIND>
-__global__ void __launch_bounds__(kPlainThreads) k_plain(const __grid_constant__ PlainArgs a) {
+constexpr int plain_min_blocks() {
+    return (V == 2 && sizeof(typename OutOf<KIND>::T) == 8) ? 10
+           : (V == 4 && sizeof(typename OutOf<KIND>::T) == 4) ? 8
+                                                               : 1;
+}
+
+template <int V, int KIND>
+__global__ void __launch_bounds__(kPlainThreads, plain_min_blocks<V, KIND>())
+    k_plain(const __grid_constant__ PlainArgs a) {
     using T = typename OutOf<KIND>::T;
     __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
     T* const out = static_cast<T*>(a.out);

@@ -5,12 +5,16 @@
 //
 //   check_kernel_math conv
 //       every v in [1, 2^31-1]: integer fp64/fp32 words == RN(double(v) *
-//       (1.0/(2^31-1))) and (float) of it; plus the SHIFTED zero.
+//       (1.0/(2^31-1))) and (float) of it; plus the SHIFTED zero.  Also the
+//       fp32 word of the kernels' FP32-pipe form (f32_bits_fp in
+//       mrg8g_device.cuh), through an exact integer emulation of its two
+//       roundings (round-toward-zero fma, round-to-nearest add).
 //   check_kernel_math leap <stream.bin> <s0..s7>
 //       stream.bin holds the oracle's outputs S[0..N) from state s; checks
 //       the window tables (S[B + o + d j] = row . s_B at B = 0) and runs every
 //       layout's decimated recurrence with the kernels' step (mad_wide_s32 +
-//       reduce_acc) over the whole stream; writes the row-major jump table to
+//       reduce_acc, and reduce_acc_alu of the 4-byte kernels) over the whole
+//       stream; writes the row-major jump table to
 //       stdout as raw u32 for the Python side to compare.
 #include <cstdio>
 #include <cstdlib>
@@ -22,6 +26,32 @@
 
 using namespace mrg8g;
 
+static int bitlen(uint64_t x) { return x ? 64 - __builtin_clzll(x) : 0; }
+
+// Float bits of f32_bits_fp(v): fh = vh 2^-15 and fl = vl 2^-31 are exact;
+// c = RZ(fh 2^-31 + fl) and f = RN(fh + c) are emulated on integers in
+// units of 2^-46 (both operands are exact multiples of it).
+static uint32_t f32_fp_emulated(uint32_t v) {
+    if (v == 0x7FFFFFBFu) return 0x3F800000u;
+    const uint64_t vh = v >> 16, vl = v & 0xFFFFu;
+    uint64_t c = (vl << 15) + vh;  // (vl + vh 2^-15) 2^-31 in units of 2^-46
+    int nb = bitlen(c);
+    if (nb > 24) c &= ~((1ull << (nb - 24)) - 1);  // round toward zero to 24 bits
+    uint64_t s = (vh << 31) + c;                   // fh + c in units of 2^-46
+    nb = bitlen(s);
+    if (nb > 24) {  // round to nearest even to 24 bits
+        const int sh = nb - 24;
+        uint64_t q = s >> sh;
+        const uint64_t rem = s & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (q & 1))) ++q;
+        s = q << sh;
+    }
+    const float f = (float)((double)s * 0x1p-46);  // exact: at most 24 significant bits
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+}
+
 static int conv() {
     const double rnorm = 1.0 / 2147483647.0;
     unsigned long bad = 0;
@@ -32,7 +62,7 @@ static int conv() {
         const float f = (float)d;
         uint32_t fb;
         std::memcpy(&fb, &f, 4);
-        if (db != f64_bits_to_p((uint32_t)v) || fb != f32_bits_of((uint32_t)v)) {
+        if (db != f64_bits_to_p((uint32_t)v) || fb != f32_bits_of((uint32_t)v) || fb != f32_fp_emulated((uint32_t)v)) {
             if (bad++ < 8) std::fprintf(stderr, "mismatch at v=%lu\n", (unsigned long)v);
         }
         // SHIFTED converts x = S - 1 = v; ORIGINAL converts v = x + 1.
@@ -40,7 +70,7 @@ static int conv() {
             bad++;
         if (f64_bits((uint32_t)v - 1, false) != db || f32_bits((uint32_t)v - 1, false) != fb) bad++;
     }
-    if (f64_bits(0, true) != 0 || f32_bits(0, true) != 0) bad++;
+    if (f64_bits(0, true) != 0 || f32_bits(0, true) != 0 || f32_fp_emulated(0) != 0) bad++;
     std::printf("conv bad=%lu\n", bad);
     return bad ? 1 : 0;
 }
@@ -73,6 +103,7 @@ static int leap(const char* path, const uint32_t s0[8]) {
                 uint64_t acc = lc.K1;
                 for (int k = 1; k <= 8; ++k) acc = mad_wide_s32(lc.c[k - 1], x[(j - k) & 7], acc);
                 const uint32_t xn = reduce_acc(acc);
+                if (reduce_acc_alu(acc) != xn) bad++;
                 x[j & 7] = xn;
                 if (xn + 1u != S[o + (size_t)d * j]) {
                     if (bad++ < 8) std::fprintf(stderr, "leap mismatch d=%d o=%d j=%zu\n", d, o, j);

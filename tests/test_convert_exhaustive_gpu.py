@@ -1,5 +1,5 @@
-"""The integer-only uniform conversion as compiled for the GPU, on every stream
-value: all S in [1, 2^31 - 1] go through the device conversion (the same
+"""The uniform conversion as compiled for the GPU (integer-only for fp64, on the
+FP32 pipes for fp32), on every stream value: all S in [1, 2^31 - 1] go through the device conversion (the same
 device functions the generators use) in both scalings, fp64 and fp32, and
 must equal IEEE round-to-nearest of (S - shift) * (1.0 / (2^31 - 1)) computed
 with the GPU's own fp64 multiply, bit for bit."""

@@ -1,5 +1,6 @@
 """CPU checks of the arithmetic the sm_103a kernels execute: the integer-only
-fp64/fp32 uniform conversion (exhaustive over all 2^31-1 stream values), the
+fp64/fp32 uniform conversion and an exact emulation of the FP32-pipe fp32
+conversion (exhaustive over all 2^31-1 stream values), the
 host-generated jump and window tables, and the decimated recurrences with the
 kernels' exact multiply-add / reduction steps, all against the oracle."""
 import os
