@@ -305,11 +305,11 @@ def run_reference(args) -> None:
         return
     import numpy as np
 
-    from oracle.pyoracle import F64_SHIFTED, REF_DIR, KIND_DTYPE, Oracle
+    from oracle.pyoracle import F64_SHIFTED, REF_DIR, KIND_DTYPE, Oracle, reference_dir
     cores = os.cpu_count() or 1
     kind_name, impl = "port", None
-    refdir = os.environ.get("MRG8_REFERENCE", "/root/reference")
-    if os.path.exists(os.path.join(REF_DIR, "libmrg8_ref_knl.so")) and os.path.isdir(refdir):
+    refdir = reference_dir()
+    if os.path.exists(os.path.join(REF_DIR, "libmrg8_ref_knl.so")) and refdir is not None:
         try:
             from oracle.pyoracle import RefLib
             impl = RefLib("knl", refdir)

@@ -66,8 +66,18 @@ public:
         return r;
     }
     double operator()() { return rand(); }
-    // cuda/mrg8.cpp:290-339: the same stream as rand().
+    // cuda/mrg8.cpp:290-339: the same values as rand(), ORIGINAL scaling
+    // (S * rnorm, in (0, 1]), which is what the mrg8 / mrg8_cuda classes of
+    // the reference's cuda/ and original/ trees return.  The reference's KNL
+    // class (knl/mrg8.h:387-436) returns SHIFTED values ((S - 1) * rnorm, in
+    // [0, 1)) from the same signature; a caller ported from there passes
+    // MRG8G_SHIFTED to the overload below.
     void mrg8dnz2(double* ran, int n) { rand(ran, n); }
+    void mrg8dnz2(double* ran, int n, int scaling) {
+        if (scaling != MRG8G_ORIGINAL && scaling != MRG8G_SHIFTED)
+            throw std::invalid_argument("mrg8dnz2: scaling must be MRG8G_ORIGINAL or MRG8G_SHIFTED");
+        host(ran, n, scaling == MRG8G_SHIFTED ? MRG8G_F64_SHIFTED : MRG8G_F64_ORIGINAL);
+    }
 
     // original/mrg8.cpp:104-129: jumps that advance this stream.
     void jump_ahead(const short jump_val_bin[200]) { mrg8g_detail::check(mrg8g_jump_ahead_bits(g_, jump_val_bin)); }

@@ -195,7 +195,9 @@ MRG8G_API int mrg8g_generate_each(const mrg8g_instance *inst, uint64_t count, vo
 
 /* Largest batch accepted by mrg8g_batch_generate_noalloc. */
 #define MRG8G_NOALLOC_MAX_INSTANCES 4096
-#define MRG8G_NOALLOC_MAX_TILES 65536 /* tiles of 512 warp rows (32K-64K outputs each) */
+/* Body tiles hold 32,768 outputs (512 warp rows of 64); an instance whose
+ * output does not start on a 16-byte boundary takes one extra head tile. */
+#define MRG8G_NOALLOC_MAX_TILES 65536
 
 /* Allocation-free form of a batch.  No reference counterpart: the reference
  * has no batches, and this entry point exists for callers that may not
@@ -211,9 +213,12 @@ MRG8G_API int mrg8g_generate_each(const mrg8g_instance *inst, uint64_t count, vo
  * instances and MRG8G_NOALLOC_MAX_TILES tiles per call (MRG8G_ERR_BUDGET
  * beyond).  The first call on a device looks up the scratch array's device
  * address (and uploads the jump tables if nothing else did), so make that
- * first call before any stream capture.  All calls share the one array: two
- * calls whose work overlaps on the GPU (different streams without ordering)
- * race; calls on the same stream are ordered. */
+ * first call before any stream capture.  The descriptors are copied from a
+ * host staging area inside the library that every call rewrites, so a call
+ * on a stream that is capturing is refused (MRG8G_ERR_INVALID_ARGUMENT,
+ * nothing enqueued).  All calls share the one array: two calls whose work
+ * overlaps on the GPU (different streams without ordering) race; calls on the
+ * same stream are ordered. */
 MRG8G_API int mrg8g_batch_generate_noalloc(const mrg8g_instance *inst, uint64_t count, void *stream);
 
 /* Time the candidate shapes on this batch (tile rows 128..2048 x 128 or 256
@@ -280,6 +285,12 @@ typedef struct mrg8g_server_stats {
     uint64_t submitted, completed, pending, launches, launched_requests, samples;
     uint64_t bytes_in_use, peak_bytes;
     int32_t error, reserved;
+    /* Most launches in flight at once (enqueued, completion not yet seen). */
+    uint64_t max_inflight;
+    /* Launches whose device execution (timed by events around the copy and
+     * kernel) overlapped that of another launch. */
+    uint64_t overlapped_launches;
+    double mean_batch; /* launched_requests / launches */
 } mrg8g_server_stats;
 
 typedef struct mrg8g_server mrg8g_server;
@@ -317,6 +328,9 @@ typedef struct mrg8g_loadtest_config {
 typedef struct mrg8g_loadtest_result {
     uint64_t requests, samples, bytes, launches, peak_bytes, late_submits;
     double wall_s, gsamples_per_s, mean_us, p50_us, p90_us, p99_us, max_us, mean_batch;
+    /* over this run: most launches in flight at once, launches that
+     * overlapped another on the device */
+    uint64_t max_inflight, overlapped_launches;
 } mrg8g_loadtest_result;
 
 MRG8G_API int mrg8g_server_loadtest(mrg8g_server *s, const mrg8g_loadtest_config *cfg, mrg8g_loadtest_result *res);

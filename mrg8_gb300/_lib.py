@@ -113,7 +113,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("pending", C.c_uint64),
                 ("launches", C.c_uint64), ("launched_requests", C.c_uint64), ("samples", C.c_uint64),
                 ("bytes_in_use", C.c_uint64), ("peak_bytes", C.c_uint64), ("error", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("max_inflight", C.c_uint64), ("overlapped_launches", C.c_uint64),
+                ("mean_batch", C.c_double)]
 
 
 class LoadtestConfig(C.Structure):
@@ -128,7 +129,8 @@ class LoadtestResult(C.Structure):
     _fields_ = [("requests", C.c_uint64), ("samples", C.c_uint64), ("bytes", C.c_uint64), ("launches", C.c_uint64),
                 ("peak_bytes", C.c_uint64), ("late_submits", C.c_uint64), ("wall_s", C.c_double),
                 ("gsamples_per_s", C.c_double), ("mean_us", C.c_double), ("p50_us", C.c_double),
-                ("p90_us", C.c_double), ("p99_us", C.c_double), ("max_us", C.c_double), ("mean_batch", C.c_double)]
+                ("p90_us", C.c_double), ("p99_us", C.c_double), ("max_us", C.c_double), ("mean_batch", C.c_double),
+                ("max_inflight", C.c_uint64), ("overlapped_launches", C.c_uint64)]
 
 
 class BatchConfig(C.Structure):

@@ -209,7 +209,10 @@ class MRG8:
         return fran
 
     def mrg8dnz2(self, ran, n=None, scaling=None):
-        """cuda/mrg8.cpp:290-339: the same stream as rand()."""
+        """cuda/mrg8.cpp:290-339: the same values as rand().  The default is
+        ORIGINAL scaling (S * rnorm), as the reference's cuda/ and original/
+        classes; scaling=SHIFTED gives (S - 1) * rnorm, as the reference's KNL
+        class (knl/mrg8.h:387-436)."""
         return self.rand(ran, n, scaling)
 
 

@@ -253,6 +253,17 @@ extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t
     if (count > MRG8G_NOALLOC_MAX_INSTANCES)
         return fail(MRG8G_ERR_BUDGET, "%llu instances exceed the no-alloc limit of %d", (unsigned long long)count,
                     MRG8G_NOALLOC_MAX_INSTANCES);
+    // A stream that is capturing would record the descriptor copy below as a
+    // graph node reading g_noalloc_host at replay time, after later calls have
+    // rewritten it; such calls are refused before anything is enqueued.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t qe = cudaStreamIsCapturing((cudaStream_t)stream, &cap);
+    if (qe != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(qe, "cudaStreamIsCapturing");
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "the no-alloc batch cannot be enqueued on a stream that is capturing");
     int dev = 0;
     int rc = ensure_device(&dev, nullptr);
     if (rc) return rc;

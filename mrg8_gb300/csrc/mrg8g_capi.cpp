@@ -151,6 +151,9 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
     tile = std::max<uint64_t>(tile, std::max<uint64_t>(D * 32, 4096));  // >= 4096 outputs and 32 rows per warp
     uint64_t warps = body ? (body + tile - 1) / tile : 1;
     const uint64_t blocks = (warps + kPlainThreads / 32 - 1) / (kPlainThreads / 32);
+    if (blocks > (uint64_t)INT32_MAX)
+        return fail(MRG8G_ERR_INVALID_ARGUMENT, "bulk launch of %llu blocks exceeds the grid limit",
+                    (unsigned long long)blocks);
 
     PlainArgs a;
     std::memcpy(a.st, st, sizeof(a.st));

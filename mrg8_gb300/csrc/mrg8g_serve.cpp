@@ -64,6 +64,8 @@ struct Slot {
     char* h_stage = nullptr;        // pinned staging of the same layout
     uint32_t* d_counter = nullptr;  // work-queue counter, finished-block counter
     cudaEvent_t done_ev = nullptr;  // recorded after the batch
+    cudaEvent_t t0_ev = nullptr;    // timing events around the copy and kernel
+    cudaEvent_t t1_ev = nullptr;
     std::vector<uint64_t> tickets;
     bool busy = false;
     mrg8g_server* server = nullptr;
@@ -95,6 +97,17 @@ struct mrg8g_server {
 
     // statistics
     uint64_t submitted = 0, finished = 0, launches = 0, launched_requests = 0, samples = 0, peak_bytes = 0;
+    uint64_t max_inflight = 0, overlapped = 0;
+    // Device intervals of the most recent finished launches (ms after
+    // base_ev), to find launches that ran on the device at the same time.
+    struct Interval {
+        float t0, t1;
+        bool counted;
+    };
+    static constexpr int kRecent = 64;
+    Interval recent[kRecent] = {};
+    int nrecent = 0, next_recent = 0;
+    cudaEvent_t base_ev = nullptr;  // recorded and completed at creation
 };
 
 namespace {
@@ -148,6 +161,7 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
     std::memcpy(sl.h_stage, insts.data(), ib);
     std::memcpy(sl.h_stage + ib, base.data(), bb);
     cudaError_t e;
+    if ((e = cudaEventRecord(sl.t0_ev, sl.stream)) != cudaSuccess) return cuda_fail(e, "serving: timing event");
     if (ntiles) {
         if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + bb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: copy of the batch descriptors");
@@ -168,13 +182,38 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
         if ((e = launch_batch(a, sv->cfg.threads, blocks, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: batch launch");
     }
-    if ((e = cudaEventRecord(sl.done_ev, sl.stream)) != cudaSuccess)
+    if ((e = cudaEventRecord(sl.t1_ev, sl.stream)) != cudaSuccess ||
+        (e = cudaEventRecord(sl.done_ev, sl.stream)) != cudaSuccess)
         return cuda_fail(e, "serving: completion event");
     return MRG8G_SUCCESS;
 }
 
+// Device interval of a finished launch against the recent ones (lock held;
+// the slot's events have completed).  A launch that overlaps an earlier one
+// counts both, once each.
+void note_interval(mrg8g_server* sv, Slot& sl) {
+    float a = 0.f, b = 0.f;
+    if (cudaEventElapsedTime(&a, sv->base_ev, sl.t0_ev) != cudaSuccess ||
+        cudaEventElapsedTime(&b, sv->base_ev, sl.t1_ev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    mrg8g_server::Interval cur{a, b, false};
+    for (int i = 0; i < sv->nrecent; ++i) {
+        mrg8g_server::Interval& o = sv->recent[i];
+        if (cur.t0 < o.t1 && o.t0 < cur.t1) {
+            if (!o.counted) o.counted = true, sv->overlapped++;
+            if (!cur.counted) cur.counted = true, sv->overlapped++;
+        }
+    }
+    sv->recent[sv->next_recent] = cur;
+    sv->next_recent = (sv->next_recent + 1) % mrg8g_server::kRecent;
+    sv->nrecent = std::min(sv->nrecent + 1, (int)mrg8g_server::kRecent);
+}
+
 // Requests of a finished slot complete at time t with status rc (lock held).
 void finish_slot(mrg8g_server* sv, Slot& sl, double t, int rc) {
+    if (rc == MRG8G_SUCCESS) note_interval(sv, sl);
     for (uint64_t tk : sl.tickets) {
         Req& q = sv->reqs[tk];
         q.t_done = t;
@@ -258,6 +297,9 @@ void scheduler(mrg8g_server* sv) {
             sl.busy = true;
             sv->launches++;
             sv->launched_requests += sl.tickets.size();
+            uint64_t busy = 0;
+            for (const Slot& o : sv->slots) busy += o.busy ? 1 : 0;
+            sv->max_inflight = std::max(sv->max_inflight, busy);
             lk.unlock();
             const int rc = enqueue_slot(sv, sl, insts, base, tile_elems);
             std::string msg = rc ? mrg8g_last_error() : "";
@@ -289,7 +331,10 @@ void destroy_server(mrg8g_server* sv) {
         if (sl.d_counter) cudaFree(sl.d_counter);
         if (sl.h_stage) cudaFreeHost(sl.h_stage);
         if (sl.done_ev) cudaEventDestroy(sl.done_ev);
+        if (sl.t0_ev) cudaEventDestroy(sl.t0_ev);
+        if (sl.t1_ev) cudaEventDestroy(sl.t1_ev);
     }
+    if (sv->base_ev) cudaEventDestroy(sv->base_ev);
     if (sv->arena_base) cudaFree(sv->arena_base);
     if (sv->d_states) cudaFree(sv->d_states);
     delete sv;
@@ -348,10 +393,17 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
             (e = cudaMalloc(&sl.d_counter, 2 * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaMemset(sl.d_counter, 0, 2 * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaHostAlloc(&sl.h_stage, stage, cudaHostAllocDefault)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess) {
+            (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreate(&sl.t0_ev)) != cudaSuccess || (e = cudaEventCreate(&sl.t1_ev)) != cudaSuccess) {
             destroy_server(sv);
             return cuda_fail(e, "serving: slot allocation");
         }
+    }
+    if ((e = cudaEventCreate(&sv->base_ev)) != cudaSuccess ||
+        (e = cudaEventRecord(sv->base_ev, sv->slots[0].stream)) != cudaSuccess ||
+        (e = cudaEventSynchronize(sv->base_ev)) != cudaSuccess) {
+        destroy_server(sv);
+        return cuda_fail(e, "serving: timing base event");
     }
     try {
         sv->thread = std::thread(scheduler, sv);
@@ -465,6 +517,10 @@ int mrg8g_server_read(mrg8g_server* sv, uint64_t ticket, void* host, uint64_t by
         if (bytes > q.bytes) return fail(MRG8G_ERR_INVALID_ARGUMENT, "read past the result");
         src = static_cast<const char*>(sv->arena_base) + q.arena_off;
     }
+    // A plain blocking copy: the request is done, i.e. the scheduler has seen
+    // the completion event of its launch, so its outputs are complete in
+    // device memory and no ordering with the launch's (non-blocking) stream is
+    // needed.  The region stays the request's until mrg8g_server_release.
     cudaError_t e = cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "serving: result read");
     return MRG8G_SUCCESS;
@@ -495,6 +551,10 @@ int mrg8g_server_get_stats(mrg8g_server* sv, mrg8g_server_stats* st) {
     st->bytes_in_use = sv->arena->used();
     st->peak_bytes = sv->peak_bytes;
     st->error = sv->error;
+    st->reserved = 0;
+    st->max_inflight = sv->max_inflight;
+    st->overlapped_launches = sv->overlapped;
+    st->mean_batch = sv->launches ? (double)sv->launched_requests / (double)sv->launches : 0.0;
     return MRG8G_SUCCESS;
 }
 
@@ -518,6 +578,12 @@ int mrg8g_server_loadtest(mrg8g_server* sv, const mrg8g_loadtest_config* cfg, mr
     std::vector<int> kinds;
     for (int k = 0; k < 5; ++k)
         if (cfg->kinds_mask & (1u << k)) kinds.push_back(k);
+    mrg8g_server_stats st0;
+    mrg8g_server_get_stats(sv, &st0);
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->max_inflight = 0;  // high-water mark of this run
+    }
     std::atomic<bool> done_submitting{false};
     std::atomic<uint64_t> submitted{0};
     std::vector<double> lat;
@@ -603,8 +669,10 @@ int mrg8g_server_loadtest(mrg8g_server* sv, const mrg8g_loadtest_config* cfg, mr
     res->p90_us = pct(0.90) * 1e6;
     res->p99_us = pct(0.99) * 1e6;
     res->max_us = lat.empty() ? 0 : lat.back() * 1e6;
-    res->launches = st.launches;
-    res->mean_batch = st.launches ? (double)st.launched_requests / st.launches : 0;
+    res->launches = st.launches - st0.launches;
+    res->mean_batch = res->launches ? (double)(st.launched_requests - st0.launched_requests) / res->launches : 0;
+    res->max_inflight = st.max_inflight;
+    res->overlapped_launches = st.overlapped_launches - st0.overlapped_launches;
     res->peak_bytes = st.peak_bytes;
     res->late_submits = late;
     return MRG8G_SUCCESS;

@@ -165,6 +165,20 @@ class Oracle:
         return tab
 
 
+def reference_dir():
+    """Directory of the reference's sources, or None: $MRG8_REFERENCE, else the
+    directory that ``make -C oracle ref REF=...`` recorded in _ref/REFDIR."""
+    env = os.environ.get("MRG8_REFERENCE")
+    if env:
+        return env if os.path.isdir(env) else None
+    try:
+        with open(os.path.join(REF_DIR, "REFDIR")) as f:
+            d = f.read().strip()
+    except OSError:
+        return None
+    return d if d and os.path.isdir(d) else None
+
+
 class RefLib:
     """One flavour of the reference compiled from its own sources."""
 

@@ -9,7 +9,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFDIR = os.environ.get("MRG8_REFERENCE", "/root/reference")
 KAT_PATH = os.path.join(ROOT, "tests", "golden", "mrg8_kat.json")
 
 
@@ -33,13 +32,15 @@ def kat():
 @pytest.fixture(scope="session")
 def reflib():
     """The reference compiled from its own sources (only where it exists)."""
-    from oracle.pyoracle import REF_DIR, RefLib
-    if not os.path.isdir(REFDIR):
-        pytest.skip("reference sources not present on this machine")
+    from oracle.pyoracle import REF_DIR, RefLib, reference_dir
+    refdir = reference_dir()
+    if refdir is None:
+        pytest.skip("reference sources not found: set MRG8_REFERENCE or build them with "
+                    "make -C oracle ref REF=<dir>")
     if not os.path.exists(os.path.join(REF_DIR, "libmrg8_ref_original.so")):
         import subprocess
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REFDIR}"], check=True)
-    return {f: RefLib(f, REFDIR) for f in RefLib.FLAVOURS}
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={refdir}"], check=True)
+    return {f: RefLib(f, refdir) for f in RefLib.FLAVOURS}
 
 
 @pytest.fixture(scope="session")

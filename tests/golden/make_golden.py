@@ -113,4 +113,6 @@ def main(refdir: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <directory of the reference's sources>")
+    main(sys.argv[1])

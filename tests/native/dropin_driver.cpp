@@ -6,6 +6,9 @@
 // include/mrg8_cuda.hpp and libmrg8g.so; prints values for the test to check.
 //   dropin_driver host   seeding and jumps only (no GPU needed)
 //   dropin_driver gpu    device and host generation through the classes
+//   dropin_driver dnz2   mrg8dnz2 in both scalings, consecutive calls on one
+//                        object: a digest of each call's values (sum over i
+//                        of word_i * (2 i + 1), mod 2^64)
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -22,8 +25,32 @@ static void print_state(const char* tag, const mrg8& m) {
     std::printf("\n");
 }
 
+static uint64_t digest(const double* v, int n) {
+    uint64_t h = 0;
+    for (int i = 0; i < n; ++i) {
+        uint64_t w;
+        std::memcpy(&w, v + i, 8);
+        h += w * (2ull * (uint64_t)i + 1ull);
+    }
+    return h;
+}
+
 int main(int argc, char** argv) {
     const uint32_t iseed = 13579;
+    if (argc > 1 && !std::strcmp(argv[1], "dnz2")) {
+        const int ns[] = {1, 1023, 1024, 1025, 3000, 1000000};
+        for (int scaling : {MRG8G_ORIGINAL, MRG8G_SHIFTED}) {
+            mrg8 m(iseed);
+            for (int n : ns) {
+                std::vector<double> v(n);
+                if (scaling == MRG8G_ORIGINAL) m.mrg8dnz2(v.data(), n);
+                else m.mrg8dnz2(v.data(), n, MRG8G_SHIFTED);
+                std::printf("dnz2_%d_%d %llu %.17g\n", scaling, n, (unsigned long long)digest(v.data(), n), v[n - 1]);
+            }
+            print_state(scaling == MRG8G_ORIGINAL ? "dnz2_state_0" : "dnz2_state_1", m);
+        }
+        return 0;
+    }
     if (argc > 1 && !std::strcmp(argv[1], "host")) {
         mrg8 m(iseed);
         print_state("seeded", m);

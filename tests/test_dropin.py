@@ -39,6 +39,30 @@ def test_dropin_host_calls(driver, oracle):
     assert [int(v) for v in rows["after_jump2^199"]] == oracle.jump_bits(j, [0] * 199 + [1]).tolist()
 
 
+def digest(a: np.ndarray) -> int:
+    """sum_i word_i * (2 i + 1) mod 2^64 over the 8-byte words of a (as the driver)."""
+    w = a.view(np.uint64)
+    with np.errstate(over="ignore"):
+        return int((w * (2 * np.arange(w.size, dtype=np.uint64) + np.uint64(1))).sum(dtype=np.uint64))
+
+
+@pytest.mark.gpu
+def test_dropin_mrg8dnz2_both_scalings(driver, oracle):
+    """mrg8::mrg8dnz2 of the compiled drop-in against the oracle's restatement
+    of cuda/mrg8.cpp:290-339 (ORIGINAL) and knl/mrg8.h:387-436 (SHIFTED), on
+    consecutive calls of sizes around the reference's 1024-deep buffer."""
+    r = subprocess.run([driver, "dnz2"], capture_output=True, text=True, check=True)
+    rows = parse(r.stdout)
+    for scaling in (0, 1):
+        st = oracle.seed(13579)
+        for n in (1, 1023, 1024, 1025, 3000, 1000000):
+            want, st = oracle.mrg8dnz2(st, n, scaling)
+            got = rows[f"dnz2_{scaling}_{n}"]
+            assert float(got[1]) == want[-1], (scaling, n)
+            assert int(got[0]) == digest(want), (scaling, n)
+        assert [int(v) for v in rows[f"dnz2_state_{scaling}"]] == st.tolist()
+
+
 @pytest.mark.gpu
 def test_dropin_device_and_host_generation(driver, oracle):
     r = subprocess.run([driver, "gpu"], capture_output=True, text=True, check=True)

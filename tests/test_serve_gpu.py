@@ -184,3 +184,48 @@ def test_sleeping_scheduler_gives_the_same_results(cuda, oracle):
             drain(srv, 1, res)
             assert np.array_equal(res[t][1].view(np.uint8), segment(oracle, seed, off, n, kind).view(np.uint8))
             time.sleep(0.004)  # longer than any spin window: the next submit wakes a sleeping thread
+
+
+def test_burst_batches_and_overlaps_on_the_device(cuda, oracle):
+    """A burst of 300 mid-size requests arriving while every in-flight slot is
+    busy: the scheduler packs them into few launches (mean batch > 1), keeps
+    several launches in flight, their device intervals (events around each
+    launch's copy and kernel) overlap, and every result still equals its
+    request's own stream segment."""
+    from mrg8_gb300.serve import Server
+    rng = np.random.default_rng(21)
+    with Server(budget_bytes=8 << 30, inflight=3, max_batch=32) as srv:
+        # One large request per slot, each launched before the next is
+        # submitted, so that all three slots are busy when the burst comes.
+        blockers = []
+        for b in range(3):
+            blockers.append(srv.submit(1 << 28, po.F64_SHIFTED, seed=900 + b))
+            deadline = time.time() + 10
+            while srv.stats()["launches"] < b + 1 and time.time() < deadline:
+                time.sleep(1e-5)
+        burst = []
+        for j in range(300):
+            kind = KINDS[j % 5]
+            n = int(2 ** rng.uniform(10, 17))
+            seed = int(rng.integers(0, 2**32))
+            off = int(rng.integers(0, 2**40))
+            burst.append((srv.submit(n, kind, seed=seed, offset=off, tag=j), seed, off, n, kind))
+        results = {}
+        deadline = time.time() + 60
+        while len(results) < 303 and time.time() < deadline:
+            for c in srv.poll(256, 2000):
+                assert c["status"] == 0
+                if c["ticket"] not in blockers:
+                    results[c["ticket"]] = srv.read(c)
+                else:
+                    results[c["ticket"]] = None
+                srv.release(c["ticket"])
+        st = srv.stats()
+    assert len(results) == 303
+    assert st["error"] == 0
+    assert st["max_inflight"] >= 2, st
+    assert st["mean_batch"] > 1.0, st
+    assert st["overlapped_launches"] >= 2, st
+    for tk, seed, off, n, kind in burst:
+        want = segment(oracle, seed, off, n, kind)
+        assert np.array_equal(results[tk].view(np.uint8), want.view(np.uint8)), (tk, n, kind)
