@@ -9,12 +9,21 @@ output (8 GiB) is larger than L2, so no flush is needed between steps.
   e2e      the same through the C ABI with a pinned HOST buffer
            (mrg8g_generate_host: device staging + D2H inside the timed region)
   roofline HBM-write roofline of the bulk kernel against MEASURED_PEAKS.json
-  cpu_baseline  the oracle port of the reference's CPU path on all host cores
+  cpu_baseline  the reference's CPU paths on the host: the block-split
+           generator on all cores (knl/mrg8_vec.h:500-525) and the scalar
+           sequential rand() of original/mrg8.cpp:231-239 on one core,
+           both through the oracle's restatement
+  batched  config 4: one batch launch vs one bulk launch per instance
+  served   config 5: Poisson 20k req/s for 60 s, plus a short rate sweep
 
 ``--impl reference`` times the reference's CPU implementation of the path
 (the build in oracle/_ref where it exists, else the oracle port) on the same
-metric.  Under torchrun each rank generates its own 2^30-output shard of one
-stream (rank r starts r * 2^30 outputs in; no collective on the data path).
+metric and workload (2^30 outputs per step), and, where the reference's GPU
+kernel was compiled from its sources (oracle/_ref/mrg8_ref_cuda.cubin), checks
+that kernel against the oracle and times it on this GPU with a clock record
+(``ref_gpu``; not part of ``value``).  Under torchrun each rank generates its
+own 2^30-output shard of one stream (rank r starts r * 2^30 outputs in; no
+collective on the data path).
 """
 from __future__ import annotations
 
@@ -37,6 +46,13 @@ METRIC = "fp64 Gsamples/s & %HBM peak at 2^30; batched vs per-call speedup; serv
 UNIT = "Gsamples/s"
 WORKLOAD = "plain MRG8 single stream: 2^30 fp64 uniforms (SHIFTED, [0,1)) from seed 13579 per GPU"
 CPU_SAMPLE_N = 1 << 28
+SCALAR_SAMPLE_N = 1 << 26
+
+
+def workload_config(n: int, ws: int) -> dict:
+    """The `config` of both arms' lines (same keys and values)."""
+    return {"workload": WORKLOAD, "n": n, "seed": SEED,
+            "l2": "each step writes 8 GiB (> 129 MB L2): no flush needed", "parallelism": f"shard{ws}"}
 
 
 def dist_env():
@@ -206,6 +222,27 @@ class ClockSampler:
                 "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
 
 
+def cpu_scalar_baseline(n: int = SCALAR_SAMPLE_N, min_seconds: float = 2.0) -> dict:
+    """The reference's scalar path on one core: the sequential rand(double*, n)
+    of original/mrg8.cpp:231-239 (ORIGINAL scaling), restated in
+    oracle/mrg8_oracle.c (orc_rand_f64); first run discarded, as the
+    reference's drivers do."""
+    from oracle.pyoracle import Oracle
+    o = Oracle()
+    st = o.seed(SEED)
+    o.rand_f64(st, n, 0)
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        o.rand_f64(st, n, 0)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds and runs >= 2:
+            break
+    return {"value": round(n * runs / el / 1e9, 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{runs} runs of {n} sequential fp64 ORIGINAL samples (original/mrg8.cpp rand), "
+                      "first run discarded"}
+
+
 def cpu_baseline(n: int, kind: int, min_seconds: float = 3.0):
     """The reference's CPU path on all host cores: the knl/ block-split
     generator (knl/mrg8_vec.h:500-525, its non-AVX A^8 recurrence), restated
@@ -282,21 +319,34 @@ def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, se
             "lengths": f"log-uniform in [1, 2^{max_log2}]", "kinds": "fp64/fp32/u32 uniform (SHIFTED)"}
 
 
-def run_served(seconds: float, rate: float = 20_000.0):
-    """Serving load: Poisson arrivals at `rate`/s for `seconds`, offsets uniform in
-    [0, 2^48), lengths log-uniform in [2^8, 2^26], kinds fp64/fp32/uint32,
-    16 GiB admission budget, results released on completion."""
-    from mrg8_gb300.serve import Server
-    with Server(budget_bytes=16 << 30) as srv:
-        srv.loadtest(rate=rate, duration_s=min(1.0, seconds), n_min=1 << 8, n_max=1 << 26, offset_max=1 << 48,
-                     kinds_mask=0b10101, rng_seed=7)  # warm-up
-        r = srv.loadtest(rate=rate, duration_s=seconds, n_min=1 << 8, n_max=1 << 26, offset_max=1 << 48,
-                         kinds_mask=0b10101, rng_seed=11)
+def _served_row(r: dict, rate: float, seconds: float) -> dict:
     return {"rate_per_s": rate, "duration_s": seconds, "requests": r["requests"],
             "gsamples_per_s": round(r["gsamples_per_s"], 3), "p50_us": round(r["p50_us"], 1),
             "p90_us": round(r["p90_us"], 1), "p99_us": round(r["p99_us"], 1), "max_us": round(r["max_us"], 1),
-            "mean_batch": round(r["mean_batch"], 2), "launches": r["launches"],
-            "peak_bytes": r["peak_bytes"], "late_submits": r["late_submits"], "budget_bytes": 16 << 30}
+            "mean_batch": round(r["mean_batch"], 2), "launches": r["launches"], "max_inflight": r["max_inflight"],
+            "overlapped_launches": r["overlapped_launches"], "peak_bytes": r["peak_bytes"],
+            "late_submits": r["late_submits"]}
+
+
+def run_served(seconds: float, rate: float = 20_000.0, sweep=(20_000.0, 50_000.0, 100_000.0, 200_000.0),
+               sweep_seconds: float = 2.0):
+    """Serving load (config 5): Poisson arrivals at `rate`/s for `seconds`,
+    offsets uniform in [0, 2^48), lengths log-uniform in [2^8, 2^26], kinds
+    fp64/fp32/uint32, 16 GiB admission budget, results released on completion;
+    then the same load for `sweep_seconds` at each rate of `sweep`, to show
+    where latency or delivered throughput stops following the offered load."""
+    from mrg8_gb300.serve import Server
+    kw = dict(n_min=1 << 8, n_max=1 << 26, offset_max=1 << 48, kinds_mask=0b10101)
+    with Server(budget_bytes=16 << 30) as srv:
+        srv.loadtest(rate=rate, duration_s=min(1.0, seconds), rng_seed=7, **kw)  # warm-up
+        r = srv.loadtest(rate=rate, duration_s=seconds, rng_seed=11, **kw)
+        rows = [_served_row(srv.loadtest(rate=q, duration_s=sweep_seconds, rng_seed=13 + i, **kw), q, sweep_seconds)
+                for i, q in enumerate(sweep)]
+    out = _served_row(r, rate, seconds)
+    out["budget_bytes"] = 16 << 30
+    out["offered_gsamples_per_s"] = round(rate * 5.39e6 / 1e9, 1)
+    out["rate_sweep"] = rows
+    return out
 
 
 def run_reference(args) -> None:
@@ -318,7 +368,7 @@ def run_reference(args) -> None:
             impl = None
     o = Oracle()
     st = o.seed(SEED)
-    n = CPU_SAMPLE_N
+    n = N_PER_RANK
     out = np.empty(n, dtype=KIND_DTYPE[F64_SHIFTED])
 
     def step():
@@ -338,14 +388,86 @@ def run_reference(args) -> None:
               + ("knl/mrg8.h rand_tp compiled from the reference" if impl is not None else
                  "oracle port of knl/mrg8_vec.h mrg8_vec_outer_tp (block split + A^8 recurrence)")
               + f", {cores} threads")
+    scalar = None if args.skip_cpu else cpu_scalar_baseline()
+    ref_gpu = None if args.skip_ref_gpu else reference_gpu_kernel()
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "n": N_PER_RANK, "seed": SEED},
+            "data": "synthetic", "config": workload_config(n, ws),
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": kind_name,
-                             "sample": sample},
-            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": sample, "scalar_original": scalar},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "ref_gpu": ref_gpu}
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernel() -> dict | None:
+    """The reference's own GPU kernel, rng_outer_32 (cuda/mrg8_cuda.cu:282-399),
+    compiled from its sources into oracle/_ref/mrg8_ref_cuda.cubin: checked
+    bit for bit against the oracle at 2^24 and timed (kernel only, CUDA
+    events) at 2^30 over the launch shapes its own driver sweeps
+    (cuda/tests/test_mrg8_outer.cu:50-76), with the SM clocks sampled
+    meanwhile.  None where the cubin was not built."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+    except ImportError:
+        return None
+    from oracle import ref_gpu_run as rg
+    if not rg.available():
+        return {"unavailable": "the reference's sources were not present where this tree was built"}
+    rg.build_driver()
+    chk = rg.check(1 << 24)
+    shapes = [(t, b) for t in (64 * 1024, 256 * 1024, 1024 * 1024) for b in (32, 64, 128, 256, 512)]
+    with ClockSampler(0) as clk:
+        rows = rg.time_shapes(1 << 30, 10, shapes)
+    best = max(rows, key=lambda r: r["gsamples_per_s"])
+    default = next(r for r in rows if r["tnum"] == 64 * 1024 and r["bs"] == 64)
+    return {"kernel": "rng_outer_32 (cuda/mrg8_cuda.cu:282-399), built from the reference sources for sm_103a",
+            "n": 1 << 30, "dtype": "f64 SHIFTED", "mismatches": chk["mismatches"], "checked_outputs": chk["n"],
+            "next_state_equal": chk["next_state_equal"], "default_shape": default, "best_shape": best,
+            "unit": UNIT, "timing": "kernel only, CUDA events, 10 launches per shape", "clocks": clk.summary()}
+
+
+def run_ceilings(args) -> None:
+    """Denominators beside the measured copy peak: the write-only HBM rate
+    (memset and fill of 8 GiB, the bulk kernel's traffic pattern being pure
+    writes) and the host link (1 GiB to and from pinned host memory, the
+    bound of the e2e figure).  CUDA events on the current stream, best of
+    `args.steps` after `args.warmup` untimed runs; SM clocks sampled."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    buf = torch.empty(1 << 30, dtype=torch.float64, device=dev)
+    host = torch.empty(1 << 27, dtype=torch.float64, pin_memory=True)
+    dsmall = buf[: 1 << 27]
+
+    def best(fn, nbytes):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(max(args.steps, 3)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return {"gbs": round(nbytes / min(ts) / 1e9, 1), "bytes": nbytes, "best_ms": round(min(ts) * 1e3, 4),
+                "median_ms": round(statistics.median(ts) * 1e3, 4)}
+
+    with ClockSampler(0) as clk:
+        out = {"memset_8GiB": best(lambda: buf.zero_(), buf.numel() * 8),
+               "fill_8GiB": best(lambda: buf.fill_(0.5), buf.numel() * 8),
+               "d2h_pinned_1GiB": best(lambda: host.copy_(dsmall, non_blocking=True), host.numel() * 8),
+               "h2d_pinned_1GiB": best(lambda: dsmall.copy_(host, non_blocking=True), host.numel() * 8)}
+    peaks, src = measured_peaks()
+    print(json.dumps({"ceilings": out, "copy_peak_gbs": peaks.get("hbm_gbs"), "copy_peak_source": src,
+                      "clocks": clk.summary(), "steps": max(args.steps, 3), "warmup": max(args.warmup, 1)}),
+          flush=True)
 
 
 def run_gpu(args) -> None:
@@ -465,14 +587,15 @@ def run_gpu(args) -> None:
     cpu = None
     if not args.skip_cpu:
         v, cores, sample = cpu_baseline(CPU_SAMPLE_N, O_F64S)
-        cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "scalar_original": cpu_scalar_baseline()}
     traffic = profiled_traffic("k_plain_f64_2p30.md")
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "seed": SEED, "layout": "1 warp tile per resident warp, V=2",
-                   "l2": "each step writes 8 GiB (> 129 MB L2): no flush needed", "parallelism": f"shard{ws}"},
+        "config": workload_config(n, ws),
+        "layout": "1 warp tile per resident warp, 2 substreams per lane",
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "peak_source": f"{peak_src} hbm_gbs (copy)",
                      "traffic": traffic, "algorithmic_bytes_per_launch": 8 * n},
@@ -492,17 +615,21 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ceilings", action="store_true", help="measure the write-only HBM and host-link ceilings")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-f32", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--skip-ref-gpu", action="store_true", help="reference arm without its GPU-kernel leg")
     ap.add_argument("--batch-count", type=int, default=10_000, help="instances of the batched leg (profiling)")
     ap.add_argument("--batch-no-tune", action="store_true", help="batched leg with the default config (profiling)")
     ap.add_argument("--n", type=int, default=N_PER_RANK, help="outputs per GPU (profiling of small cases)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.ceilings:
+        run_ceilings(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -287,8 +287,9 @@ typedef struct mrg8g_server_stats {
     int32_t error, reserved;
     /* Most launches in flight at once (enqueued, completion not yet seen). */
     uint64_t max_inflight;
-    /* Launches whose device execution (timed by events around the copy and
-     * kernel) overlapped that of another launch. */
+    /* Launches whose kernel ran on the device at the same time as another
+     * launch's kernel (intervals from the device's global timer, stamped by
+     * the kernel's first and last blocks). */
     uint64_t overlapped_launches;
     double mean_batch; /* launched_requests / launches */
 } mrg8g_server_stats;
@@ -329,7 +330,7 @@ typedef struct mrg8g_loadtest_result {
     uint64_t requests, samples, bytes, launches, peak_bytes, late_submits;
     double wall_s, gsamples_per_s, mean_us, p50_us, p90_us, p99_us, max_us, mean_batch;
     /* over this run: most launches in flight at once, launches that
-     * overlapped another on the device */
+     * overlapped another on the device (peak_bytes is this run's too) */
     uint64_t max_inflight, overlapped_launches;
 } mrg8g_loadtest_result;
 

@@ -73,8 +73,15 @@ __device__ __forceinline__ BatchTile derive_tile(const BatchArgs& a, uint32_t ti
     return t;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ BatchArgs a) {
+    if (a.times && blockIdx.x == 0 && threadIdx.x == 0) a.times[0] = global_ns();
     __shared__ uint32_t scratch[THREADS / 32][8 * kBatchLayoutV * 32];
     // The A^(2^i) table in shared memory: a block's tiles jump from here
     // instead of from L2, whose latency a short tile cannot hide.
@@ -131,6 +138,10 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
         if (threadIdx.x == 0 && atomicAdd(a.done_blocks, 1u) == gridDim.x - 1) {
             *a.counter = 0;
             *a.done_blocks = 0;
+            if (a.times) {
+                a.times[1] = global_ns();
+                __threadfence_system();
+            }
         }
     }
 }
@@ -314,6 +325,7 @@ extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t
     a.ninst = count;
     a.tile_elems = 0;
     a.states = nullptr;
+    a.times = nullptr;
     for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
     const int sms = device_sms();
     const uint64_t want = (ntiles + 3) / 4;

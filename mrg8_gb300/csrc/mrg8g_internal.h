@@ -65,6 +65,9 @@ struct BatchArgs {
     uint32_t* done_blocks;    // null, or blocks finished: the last block then
                               // zeroes *counter and *done_blocks for the next launch
     const uint32_t* states;   // generator table (8 words per slot) or null
+    unsigned long long* times;  // null, or [start, end] of the launch in
+                                // %globaltimer ns (block 0's start, the last
+                                // block's end), written for the serving stats
     LeapCoef leap[kNumLayouts];
 };
 

@@ -64,8 +64,10 @@ struct Slot {
     char* h_stage = nullptr;        // pinned staging of the same layout
     uint32_t* d_counter = nullptr;  // work-queue counter, finished-block counter
     cudaEvent_t done_ev = nullptr;  // recorded after the batch
-    cudaEvent_t t0_ev = nullptr;    // timing events around the copy and kernel
-    cudaEvent_t t1_ev = nullptr;
+    // [start, end] of the slot's kernel in %globaltimer ns, written by the
+    // kernel into mapped pinned host memory (no API call on the launch path).
+    volatile unsigned long long* h_times = nullptr;
+    unsigned long long* d_times = nullptr;
     std::vector<uint64_t> tickets;
     bool busy = false;
     mrg8g_server* server = nullptr;
@@ -98,16 +100,15 @@ struct mrg8g_server {
     // statistics
     uint64_t submitted = 0, finished = 0, launches = 0, launched_requests = 0, samples = 0, peak_bytes = 0;
     uint64_t max_inflight = 0, overlapped = 0;
-    // Device intervals of the most recent finished launches (ms after
-    // base_ev), to find launches that ran on the device at the same time.
+    // Kernel intervals of the most recent finished launches (%globaltimer
+    // ns), to find launches that ran on the device at the same time.
     struct Interval {
-        float t0, t1;
+        unsigned long long t0, t1;
         bool counted;
     };
     static constexpr int kRecent = 64;
     Interval recent[kRecent] = {};
     int nrecent = 0, next_recent = 0;
-    cudaEvent_t base_ev = nullptr;  // recorded and completed at creation
 };
 
 namespace {
@@ -161,7 +162,8 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
     std::memcpy(sl.h_stage, insts.data(), ib);
     std::memcpy(sl.h_stage + ib, base.data(), bb);
     cudaError_t e;
-    if ((e = cudaEventRecord(sl.t0_ev, sl.stream)) != cudaSuccess) return cuda_fail(e, "serving: timing event");
+    sl.h_times[0] = 0;
+    sl.h_times[1] = 0;
     if (ntiles) {
         if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + bb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: copy of the batch descriptors");
@@ -175,6 +177,7 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
         a.counter = sl.d_counter;
         a.done_blocks = sl.d_counter + 1;  // the kernel leaves both at zero
         a.states = sv->d_states;
+        a.times = sl.d_times;
         for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
         const uint64_t wpb = (uint64_t)sv->cfg.threads / 32;
         const uint64_t want = (ntiles + wpb - 1) / wpb;
@@ -182,22 +185,18 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
         if ((e = launch_batch(a, sv->cfg.threads, blocks, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: batch launch");
     }
-    if ((e = cudaEventRecord(sl.t1_ev, sl.stream)) != cudaSuccess ||
-        (e = cudaEventRecord(sl.done_ev, sl.stream)) != cudaSuccess)
+    if ((e = cudaEventRecord(sl.done_ev, sl.stream)) != cudaSuccess)
         return cuda_fail(e, "serving: completion event");
     return MRG8G_SUCCESS;
 }
 
-// Device interval of a finished launch against the recent ones (lock held;
-// the slot's events have completed).  A launch that overlaps an earlier one
-// counts both, once each.
+// Kernel interval of a finished launch against the recent ones (lock held;
+// the launch's completion event has been seen, so the kernel's stamps are
+// in host memory).  A launch that overlaps an earlier one counts both, once
+// each.  Launches without a kernel (no tiles) have no stamps.
 void note_interval(mrg8g_server* sv, Slot& sl) {
-    float a = 0.f, b = 0.f;
-    if (cudaEventElapsedTime(&a, sv->base_ev, sl.t0_ev) != cudaSuccess ||
-        cudaEventElapsedTime(&b, sv->base_ev, sl.t1_ev) != cudaSuccess) {
-        cudaGetLastError();
-        return;
-    }
+    const unsigned long long a = sl.h_times[0], b = sl.h_times[1];
+    if (a == 0 || b < a) return;
     mrg8g_server::Interval cur{a, b, false};
     for (int i = 0; i < sv->nrecent; ++i) {
         mrg8g_server::Interval& o = sv->recent[i];
@@ -331,10 +330,8 @@ void destroy_server(mrg8g_server* sv) {
         if (sl.d_counter) cudaFree(sl.d_counter);
         if (sl.h_stage) cudaFreeHost(sl.h_stage);
         if (sl.done_ev) cudaEventDestroy(sl.done_ev);
-        if (sl.t0_ev) cudaEventDestroy(sl.t0_ev);
-        if (sl.t1_ev) cudaEventDestroy(sl.t1_ev);
+        if (sl.h_times) cudaFreeHost((void*)sl.h_times);
     }
-    if (sv->base_ev) cudaEventDestroy(sv->base_ev);
     if (sv->arena_base) cudaFree(sv->arena_base);
     if (sv->d_states) cudaFree(sv->d_states);
     delete sv;
@@ -393,17 +390,21 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
             (e = cudaMalloc(&sl.d_counter, 2 * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaMemset(sl.d_counter, 0, 2 * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaHostAlloc(&sl.h_stage, stage, cudaHostAllocDefault)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess ||
-            (e = cudaEventCreate(&sl.t0_ev)) != cudaSuccess || (e = cudaEventCreate(&sl.t1_ev)) != cudaSuccess) {
+            (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess) {
             destroy_server(sv);
             return cuda_fail(e, "serving: slot allocation");
         }
-    }
-    if ((e = cudaEventCreate(&sv->base_ev)) != cudaSuccess ||
-        (e = cudaEventRecord(sv->base_ev, sv->slots[0].stream)) != cudaSuccess ||
-        (e = cudaEventSynchronize(sv->base_ev)) != cudaSuccess) {
-        destroy_server(sv);
-        return cuda_fail(e, "serving: timing base event");
+        void* ht = nullptr;
+        if ((e = cudaHostAlloc(&ht, 2 * sizeof(unsigned long long), cudaHostAllocMapped)) != cudaSuccess) {
+            destroy_server(sv);
+            return cuda_fail(e, "serving: slot allocation");
+        }
+        sl.h_times = static_cast<volatile unsigned long long*>(ht);
+        sl.h_times[0] = sl.h_times[1] = 0;
+        if ((e = cudaHostGetDevicePointer((void**)&sl.d_times, ht, 0)) != cudaSuccess) {
+            destroy_server(sv);
+            return cuda_fail(e, "serving: mapped timing words");
+        }
     }
     try {
         sv->thread = std::thread(scheduler, sv);
@@ -582,7 +583,8 @@ int mrg8g_server_loadtest(mrg8g_server* sv, const mrg8g_loadtest_config* cfg, mr
     mrg8g_server_get_stats(sv, &st0);
     {
         std::lock_guard<std::mutex> lk(sv->mu);
-        sv->max_inflight = 0;  // high-water mark of this run
+        sv->max_inflight = 0;  // high-water marks of this run
+        sv->peak_bytes = sv->arena->used();
     }
     std::atomic<bool> done_submitting{false};
     std::atomic<uint64_t> submitted{0};
