@@ -368,7 +368,7 @@ def run_reference(args) -> None:
             impl = None
     o = Oracle()
     st = o.seed(SEED)
-    n = N_PER_RANK
+    n = args.n
     out = np.empty(n, dtype=KIND_DTYPE[F64_SHIFTED])
 
     def step():
@@ -388,7 +388,7 @@ def run_reference(args) -> None:
               + ("knl/mrg8.h rand_tp compiled from the reference" if impl is not None else
                  "oracle port of knl/mrg8_vec.h mrg8_vec_outer_tp (block split + A^8 recurrence)")
               + f", {cores} threads")
-    scalar = None if args.skip_cpu else cpu_scalar_baseline()
+    scalar = None if args.skip_cpu else cpu_scalar_baseline(min(SCALAR_SAMPLE_N, n))
     ref_gpu = None if args.skip_ref_gpu else reference_gpu_kernel()
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3),

@@ -110,6 +110,7 @@ def test_argument_errors(lib):
     assert lib.mrg8g_rand(g.handle, C.c_void_p(0), 10, 7, None) == L.ERR_INVALID_ARGUMENT
     assert lib.mrg8g_convert(C.c_void_p(0), C.c_void_p(0), 10, 0, None) == L.ERR_INVALID_ARGUMENT
     assert lib.mrg8g_generate(g.handle, C.c_void_p(0), 0, 1, None) == L.SUCCESS  # n = 0 is a no-op
+    assert lib.mrg8g_generate(g.handle, C.c_void_p(0), (1 << 62) + 1, 1, None) == L.ERR_INVALID_ARGUMENT
     with pytest.raises(ValueError):
         m.MRG8Cuda(1).mrg8_outer_32(np.zeros(4), 4, 48, 1024)
     with pytest.raises(ValueError):
