@@ -14,6 +14,8 @@ output (8 GiB) is larger than L2, so no flush is needed between steps.
            sequential rand() of original/mrg8.cpp:231-239 on one core,
            both through the oracle's restatement
   batched  config 4: one batch launch vs one bulk launch per instance
+  jump_stress  config 3: 65,536 device jumps by offsets in [0, 2^63), and
+           4,096 uint32 outputs after each in one batch launch
   served   config 5: Poisson 20k req/s for 60 s, plus a short rate sweep
 
 ``--impl reference`` times the reference's CPU implementation of the path
@@ -319,6 +321,46 @@ def run_batched(dev, steps: int = 5, count: int = 10_000, max_log2: int = 22, se
             "lengths": f"log-uniform in [1, 2^{max_log2}]", "kinds": "fp64/fp32/u32 uniform (SHIFTED)"}
 
 
+def run_jumps(dev, reps: int = 5, count: int = 65_536, n: int = 4096, seed: int = 20240331) -> dict:
+    """Config 3: 65,536 substreams of seed 13579, each jumped by an offset drawn
+    uniformly in [0, 2^63), with 4,096 uint32 outputs each (2^28 outputs,
+    1 GiB): the device jumps alone (mrg8g_jump_states, one warp per offset)
+    and the whole workload as one batch launch (a jump per tile, then the
+    outputs).  Both are checked bit for bit in tests/test_batch_gpu.py."""
+    import numpy as np
+    import torch
+
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(seed)
+    st = m.seed_state(SEED)
+    offs = rng.integers(0, 2**63, count, dtype=np.int64)
+    d_off = torch.from_numpy(offs).to(dev)
+    out = torch.empty((count, n), dtype=torch.int32, device=dev)
+    b = m.Batch([(st, int(offs[i]), out[i], m.U32) for i in range(count)])
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    tj = timed(lambda: m.jump_states(st, d_off))
+    tb = timed(b.launch)
+    b.close()
+    del out
+    torch.cuda.empty_cache()
+    return {"substreams": count, "outputs_each": n, "offsets": "uniform in [0, 2^63)",
+            "jumps_per_s": round(count / tj, 1), "jump_ms": round(tj * 1e3, 4),
+            "batch_ms": round(tb * 1e3, 4), "batch_gsamples_per_s": round(count * n / tb / 1e9, 3)}
+
+
 def _served_row(r: dict, rate: float, seconds: float) -> dict:
     return {"rate_per_s": rate, "duration_s": seconds, "requests": r["requests"],
             "gsamples_per_s": round(r["gsamples_per_s"], 3), "p50_us": round(r["p50_us"], 1),
@@ -572,6 +614,7 @@ def run_gpu(args) -> None:
         del host
 
     batched = None if args.skip_batch or rank else run_batched(dev, count=args.batch_count, tune=not args.batch_no_tune)
+    jumps = None if args.skip_batch or rank else run_jumps(dev)
     served = None if args.skip_serve or rank else run_served(args.serve_seconds)
 
     # Spot check of this run's output against the oracle (first 2^20 values).
@@ -600,7 +643,7 @@ def run_gpu(args) -> None:
                      "frac": round(achieved / hbm, 4), "peak_source": f"{peak_src} hbm_gbs (copy)",
                      "traffic": traffic, "algorithmic_bytes_per_launch": 8 * n},
         "f32": f32,
-        "e2e": e2e, "cpu_baseline": cpu, "batched": batched, "served": served,
+        "e2e": e2e, "cpu_baseline": cpu, "batched": batched, "jump_stress": jumps, "served": served,
         "clocks": clk.summary(), "gpu_launches": args.steps,
         "parity_spot_check": ok, "wall_s": round(wall, 4),
     }
