@@ -20,12 +20,13 @@ namespace mrg8g {
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_plain)
 
 // Resident blocks the register allocation must allow: eight for 4-byte
-// outputs with four substreams per lane (64 registers), else no bound (fp64
-// with two substreams measured 791 Goutputs/s unbounded, 56 registers, and
-// 772 when held to 48 registers for ten blocks per SM).
+// outputs with four substreams per lane (64 registers); nine for fp64
+// ORIGINAL with two (56 registers instead of 64: 718 against 710
+// Goutputs/s); else no bound (fp64 SHIFTED measured 791 Goutputs/s
+// unbounded, 56 registers, and 772 when held to 48 for ten blocks per SM).
 template <int V, int KIND>
 constexpr int plain_min_blocks() {
-    return (V == 4 && sizeof(typename OutOf<KIND>::T) == 4) ? 8 : 1;
+    return (V == 4 && sizeof(typename OutOf<KIND>::T) == 4) ? 8 : (V == 2 && KIND == kF64Orig) ? 9 : 1;
 }
 
 template <int V, int KIND>
