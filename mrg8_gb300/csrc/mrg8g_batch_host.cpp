@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <exception>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -45,6 +46,20 @@ void sort_largest_first(BatchInst* insts, uint32_t count) {
     });
 }
 
+// Tiles of a plan with body tiles of tile_elems outputs (both tilings cut the
+// instances the same way), counted without building them.
+uint64_t count_tiles(const BatchInst* insts, uint32_t count, uint64_t tile_elems) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const BatchInst& d = insts[i];
+        if (!d.n) continue;
+        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
+        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
+        total += (head ? 1 : 0) + (d.n - head + tile_elems - 1) / tile_elems;
+    }
+    return total;
+}
+
 uint64_t tile_prefix(const BatchInst* insts, uint32_t count, uint64_t tile_elems, uint32_t* base) {
     uint64_t total = 0;
     for (uint32_t i = 0; i < count; ++i) {
@@ -83,6 +98,9 @@ struct mrg8g_batch {
 namespace {
 
 constexpr int kDefaultTileRows = 512;
+// Host-listed tiles are 16 bytes each on the host and the device; above this
+// many a plan must use the derived tiling (O(instances) descriptors).
+constexpr uint64_t kMaxListedTiles = 1ull << 26;
 
 void release_graph(mrg8g_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -150,11 +168,24 @@ int upload_tiles(mrg8g_batch* b) {
     return MRG8G_SUCCESS;
 }
 
+// Validates c completely before changing the plan: a configuration that is
+// refused leaves the previous plan and configuration in place.
 int apply_config(mrg8g_batch* b, const mrg8g_batch_config& c) {
     mrg8g_batch_config n = c;
     int rc = normalise(n);
     if (rc) return rc;
     const bool retile = n.tile_rows != b->cfg.tile_rows || n.tiling != b->cfg.tiling || !b->planned;
+    if (retile) {
+        const uint64_t total =
+            count_tiles(b->insts.data(), (uint32_t)b->insts.size(), (uint64_t)n.tile_rows * 32 * kBatchLayoutV);
+        if (total > 0xFFFFFFFFull)
+            return fail(MRG8G_ERR_INVALID_ARGUMENT, "%llu tiles: more than 2^32-1; raise tile_rows",
+                        (unsigned long long)total);
+        if (!n.tiling && total > kMaxListedTiles)
+            return fail(MRG8G_ERR_INVALID_ARGUMENT,
+                        "%llu tiles exceed the %llu of a host-listed plan; use tiling = 1 or more tile_rows",
+                        (unsigned long long)total, (unsigned long long)kMaxListedTiles);
+    }
     b->cfg = n;
     if (retile) {
         b->planned = false;
@@ -238,10 +269,21 @@ void destroy_plan(mrg8g_batch* b) {
 
 }  // namespace
 
-extern "C" {
+// Host allocation failures inside the planners come back as status codes
+// (no exception crosses the C ABI).
+template <class F>
+static int guarded(F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(MRG8G_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(MRG8G_ERR_INVALID_STATE, "%s", e.what());
+    }
+}
 
-int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_batch_config* cfg,
-                       mrg8g_batch** out) {
+static int batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_batch_config* cfg,
+                        mrg8g_batch** out) {
     if (!out) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null output pointer");
     *out = nullptr;
     if (count && !inst) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null instance array");
@@ -305,38 +347,8 @@ int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_b
     return MRG8G_SUCCESS;
 }
 
-int mrg8g_batch_launch(mrg8g_batch* b, void* stream) {
-    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
-    if (!b->ntiles) return MRG8G_SUCCESS;
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!b->cfg.use_graph) return enqueue(b, s);
-    int rc;
-    if (!b->exec && (rc = build_graph(b))) return rc;
-    cudaError_t e = cudaGraphLaunch(b->exec, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
-    return MRG8G_SUCCESS;
-}
 
-int mrg8g_batch_get_config(const mrg8g_batch* b, mrg8g_batch_config* cfg) {
-    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
-    *cfg = b->cfg;
-    return MRG8G_SUCCESS;
-}
-
-int mrg8g_batch_set_config(mrg8g_batch* b, const mrg8g_batch_config* cfg) {
-    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
-    return apply_config(b, *cfg);
-}
-
-int mrg8g_batch_stats(const mrg8g_batch* b, uint64_t* tiles, uint64_t* outputs, uint64_t* bytes) {
-    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
-    if (tiles) *tiles = b->ntiles;
-    if (outputs) *outputs = b->outputs;
-    if (bytes) *bytes = b->bytes;
-    return MRG8G_SUCCESS;
-}
-
-int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chosen) {
+static int batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chosen) {
     if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
     if (!b->ntiles) {
         if (chosen) *chosen = b->cfg;
@@ -357,7 +369,13 @@ int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chose
         for (int t : threads) {
           for (int tiling = 0; tiling < 2; ++tiling) {
             mrg8g_batch_config c{r, t, 0, use_graph, tiling};
-            if ((rc = apply_config(b, c))) break;
+            if ((rc = apply_config(b, c))) {
+                if (rc == MRG8G_ERR_INVALID_ARGUMENT) {  // too many tiles for this shape
+                    rc = MRG8G_SUCCESS;
+                    continue;
+                }
+                break;
+            }
             if ((rc = mrg8g_batch_launch(b, s))) break;  // warm-up (and graph build)
             cudaEventRecord(e0, s);
             for (int k = 0; k < 3 && !rc; ++k) rc = mrg8g_batch_launch(b, s);
@@ -380,6 +398,50 @@ int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chose
     if ((rc = apply_config(b, best))) return rc;
     if (chosen) *chosen = best;
     return MRG8G_SUCCESS;
+}
+
+
+extern "C" {
+
+int mrg8g_batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_batch_config* cfg,
+                       mrg8g_batch** out) {
+    return guarded([&] { return batch_create(inst, count, cfg, out); });
+}
+
+int mrg8g_batch_launch(mrg8g_batch* b, void* stream) {
+    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
+    if (!b->planned) return fail(MRG8G_ERR_INVALID_STATE, "the batch has no valid plan (a re-plan failed)");
+    if (!b->ntiles) return MRG8G_SUCCESS;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!b->cfg.use_graph) return enqueue(b, s);
+    int rc;
+    if (!b->exec && (rc = build_graph(b))) return rc;
+    cudaError_t e = cudaGraphLaunch(b->exec, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_get_config(const mrg8g_batch* b, mrg8g_batch_config* cfg) {
+    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    *cfg = b->cfg;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_set_config(mrg8g_batch* b, const mrg8g_batch_config* cfg) {
+    if (!b || !cfg) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null pointer");
+    return guarded([&] { return apply_config(b, *cfg); });
+}
+
+int mrg8g_batch_stats(const mrg8g_batch* b, uint64_t* tiles, uint64_t* outputs, uint64_t* bytes) {
+    if (!b) return fail(MRG8G_ERR_INVALID_ARGUMENT, "null batch");
+    if (tiles) *tiles = b->ntiles;
+    if (outputs) *outputs = b->outputs;
+    if (bytes) *bytes = b->bytes;
+    return MRG8G_SUCCESS;
+}
+
+int mrg8g_batch_autotune(mrg8g_batch* b, void* stream, mrg8g_batch_config* chosen) {
+    return guarded([&] { return batch_autotune(b, stream, chosen); });
 }
 
 int mrg8g_generate_each(const mrg8g_instance* inst, uint64_t count, void* stream) {

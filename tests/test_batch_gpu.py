@@ -213,3 +213,38 @@ def test_jump_stress_65536_substreams(cuda, oracle):
         want, _ = oracle.randint(oracle.jump_matvec(st, int(offs[i])), n)
         assert np.array_equal(host[i], want), i
     b.close()
+
+
+def test_plan_limits_and_refused_configs_keep_the_plan(cuda):
+    """An instance of 2^45 outputs needs 2^30 body tiles: a host-listed plan is
+    refused before anything is built, the derived tiling plans it with
+    O(instances) descriptors, and a refused re-plan leaves that plan and its
+    configuration in place.  Through the C ABI (the Python mirror already
+    refuses an n beyond its tensor); never launched, the output buffer being a
+    stand-in."""
+    import ctypes as C
+
+    import torch
+
+    import mrg8_gb300 as m
+    from mrg8_gb300 import _lib as L
+    lib = m.load()
+    buf = torch.empty(1024, dtype=torch.int32, device=cuda)
+    inst = L.Instance()
+    inst.state[:] = [int(v) for v in m.seed_state(3)]
+    inst.offset, inst.n, inst.out, inst.kind, inst.reserved = 0, 1 << 45, buf.data_ptr(), L.U32, 0
+    arr = (L.Instance * 1)(inst)
+    h = C.c_void_p()
+    listed = L.BatchConfig(512, 128, 0, 1, 0)
+    assert lib.mrg8g_batch_create(arr, 1, C.byref(listed), C.byref(h)) == L.ERR_INVALID_ARGUMENT
+    assert b"tiling = 1" in lib.mrg8g_last_error()
+    derived = L.BatchConfig(512, 128, 0, 1, 1)
+    assert lib.mrg8g_batch_create(arr, 1, C.byref(derived), C.byref(h)) == 0, lib.mrg8g_last_error()
+    tiles = C.c_uint64()
+    assert lib.mrg8g_batch_stats(h, C.byref(tiles), None, None) == 0
+    assert tiles.value == (1 << 45) // (512 * 64)
+    assert lib.mrg8g_batch_set_config(h, C.byref(listed)) == L.ERR_INVALID_ARGUMENT
+    got = L.BatchConfig()
+    assert lib.mrg8g_batch_get_config(h, C.byref(got)) == 0
+    assert (got.tile_rows, got.tiling) == (512, 1)
+    assert lib.mrg8g_batch_destroy(h) == 0
