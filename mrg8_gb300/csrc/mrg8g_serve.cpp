@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <exception>
 #include <array>
 #include <atomic>
 #include <chrono>
@@ -230,7 +231,23 @@ void finish_slot(mrg8g_server* sv, Slot& sl, double t, int rc) {
 // cfg.spin_us after the last activity, so that requests arriving at a steady
 // rate find it awake; after that it sleeps on cv_sched.
 
+void scheduler_loop(mrg8g_server* sv);
+
+// The scheduler thread: its loop, with a host allocation failure turned into
+// a failed server (later submissions are refused; waiters time out) instead of
+// an exception that would end the process.
 void scheduler(mrg8g_server* sv) {
+    try {
+        scheduler_loop(sv);
+    } catch (const std::exception& e) {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->error = MRG8G_ERR_OUT_OF_MEMORY;
+        sv->error_msg = std::string("scheduler: ") + e.what();
+        sv->cv_done.notify_all();
+    }
+}
+
+void scheduler_loop(mrg8g_server* sv) {
     cudaSetDevice(sv->dev);
     std::vector<BatchInst> insts;
     std::vector<uint32_t> base;
@@ -471,8 +488,14 @@ int mrg8g_server_submit(mrg8g_server* sv, const mrg8g_request* r, uint64_t* tick
         sv->gen_pos[r->generator] += r->n;
     }
     const uint64_t tk = sv->next_ticket++;
-    sv->reqs.emplace(tk, q);
-    sv->pending.push_back(tk);
+    try {
+        sv->reqs.emplace(tk, q);
+        sv->pending.push_back(tk);
+    } catch (const std::bad_alloc&) {
+        sv->reqs.erase(tk);
+        if (r->generator != MRG8G_NO_GENERATOR) sv->gen_pos[r->generator] -= r->n;
+        return fail(MRG8G_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
     sv->submitted++;
     sv->wake_seq.fetch_add(1, std::memory_order_release);
     sv->cv_sched.notify_one();
