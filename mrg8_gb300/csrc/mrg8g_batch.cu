@@ -133,12 +133,17 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
     }
     // Self-resetting queue: once every block has left the loop, no warp
     // reads the counter again in this launch.
+    // Every thread's outputs are made visible device-wide before its block
+    // counts itself finished, so that when the last block stamps the end of
+    // the launch into host memory, the host may take the outputs as complete.
     if (a.done_blocks) {
+        __threadfence();
         __syncthreads();
         if (threadIdx.x == 0 && atomicAdd(a.done_blocks, 1u) == gridDim.x - 1) {
             *a.counter = 0;
             *a.done_blocks = 0;
             if (a.times) {
+                __threadfence();
                 a.times[1] = global_ns();
                 __threadfence_system();
             }

@@ -69,6 +69,8 @@ struct Slot {
     // kernel into mapped pinned host memory (no API call on the launch path).
     volatile unsigned long long* h_times = nullptr;
     unsigned long long* d_times = nullptr;
+    bool has_kernel = false;  // the launch has a kernel, which stamps its end
+    uint32_t polls = 0;       // completion checks since the launch
     std::vector<uint64_t> tickets;
     bool busy = false;
     mrg8g_server* server = nullptr;
@@ -165,6 +167,8 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
     cudaError_t e;
     sl.h_times[0] = 0;
     sl.h_times[1] = 0;
+    sl.has_kernel = ntiles != 0;
+    sl.polls = 0;
     if (ntiles) {
         if ((e = cudaMemcpyAsync(sl.d_stage, sl.h_stage, ib + bb, cudaMemcpyHostToDevice, sl.stream)) != cudaSuccess)
             return cuda_fail(e, "serving: copy of the batch descriptors");
@@ -265,9 +269,19 @@ void scheduler_loop(mrg8g_server* sv) {
     while (!sv->stop.load(std::memory_order_acquire)) {
         // In-flight launches, polled without the lock (the scheduler thread
         // owns the slots while they are busy).
+        // A launch is complete when its kernel's end stamp reaches host
+        // memory (the kernel makes all its outputs visible first), which the
+        // host sees sooner than the completion event; the event is still
+        // queried every few checks, and for launches without a kernel, so
+        // that an execution error is reported.
         done.clear();
         for (Slot& sl : sv->slots) {
             if (!sl.busy) continue;
+            if (sl.has_kernel && sl.h_times[1] != 0) {
+                done.push_back({sl.idx, now_s(), cudaSuccess});
+                continue;
+            }
+            if (sl.has_kernel && (++sl.polls & 15u) != 0) continue;
             const cudaError_t q = cudaEventQuery(sl.done_ev);
             if (q != cudaErrorNotReady) done.push_back({sl.idx, now_s(), q});
         }
