@@ -366,7 +366,8 @@ def _served_row(r: dict, rate: float, seconds: float) -> dict:
             "gsamples_per_s": round(r["gsamples_per_s"], 3), "p50_us": round(r["p50_us"], 1),
             "p90_us": round(r["p90_us"], 1), "p99_us": round(r["p99_us"], 1), "max_us": round(r["max_us"], 1),
             "mean_batch": round(r["mean_batch"], 2), "launches": r["launches"], "max_inflight": r["max_inflight"],
-            "overlapped_launches": r["overlapped_launches"], "peak_bytes": r["peak_bytes"],
+            "overlapped_launches": r["overlapped_launches"], "mean_kernel_us": round(r["mean_kernel_us"], 2),
+            "peak_bytes": r["peak_bytes"],
             "late_submits": r["late_submits"]}
 
 

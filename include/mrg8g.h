@@ -292,6 +292,9 @@ typedef struct mrg8g_server_stats {
      * the kernel's first and last blocks). */
     uint64_t overlapped_launches;
     double mean_batch; /* launched_requests / launches */
+    /* Device time of the launches with a kernel, first block's start to last
+     * block's end (global timer), summed, and how many launches it covers. */
+    uint64_t kernel_ns, kernel_launches;
 } mrg8g_server_stats;
 
 typedef struct mrg8g_server mrg8g_server;
@@ -332,6 +335,8 @@ typedef struct mrg8g_loadtest_result {
     /* over this run: most launches in flight at once, launches that
      * overlapped another on the device (peak_bytes is this run's too) */
     uint64_t max_inflight, overlapped_launches;
+    /* mean device time of this run's launches (kernel_ns / kernel_launches) */
+    double mean_kernel_us;
 } mrg8g_loadtest_result;
 
 MRG8G_API int mrg8g_server_loadtest(mrg8g_server *s, const mrg8g_loadtest_config *cfg, mrg8g_loadtest_result *res);

@@ -114,7 +114,7 @@ class ServerStats(C.Structure):
                 ("launches", C.c_uint64), ("launched_requests", C.c_uint64), ("samples", C.c_uint64),
                 ("bytes_in_use", C.c_uint64), ("peak_bytes", C.c_uint64), ("error", C.c_int32),
                 ("reserved", C.c_int32), ("max_inflight", C.c_uint64), ("overlapped_launches", C.c_uint64),
-                ("mean_batch", C.c_double)]
+                ("mean_batch", C.c_double), ("kernel_ns", C.c_uint64), ("kernel_launches", C.c_uint64)]
 
 
 class LoadtestConfig(C.Structure):
@@ -130,7 +130,7 @@ class LoadtestResult(C.Structure):
                 ("peak_bytes", C.c_uint64), ("late_submits", C.c_uint64), ("wall_s", C.c_double),
                 ("gsamples_per_s", C.c_double), ("mean_us", C.c_double), ("p50_us", C.c_double),
                 ("p90_us", C.c_double), ("p99_us", C.c_double), ("max_us", C.c_double), ("mean_batch", C.c_double),
-                ("max_inflight", C.c_uint64), ("overlapped_launches", C.c_uint64)]
+                ("max_inflight", C.c_uint64), ("overlapped_launches", C.c_uint64), ("mean_kernel_us", C.c_double)]
 
 
 class BatchConfig(C.Structure):

@@ -5,8 +5,8 @@
 // The host cuts every instance into tiles (a short unaligned head tile plus
 // body tiles of a tuned number of rows), longest instances first.  Resident
 // warps pull tile indices from a device counter; each tile jumps the
-// instance's state to the tile's first output with the resident A^(2^i)
-// table and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so
+// instance's state to the tile's first output with the resident byte-window
+// jump table and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so
 // every instance's values equal its own sequential stream.  This replaces
 // one mrg8_cuda::mrg8_outer_32 launch per instance (cuda/mrg8_cuda.cu:414-436).
 #include <algorithm>
@@ -83,12 +83,6 @@ template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ BatchArgs a) {
     if (a.times && blockIdx.x == 0 && threadIdx.x == 0) a.times[0] = global_ns();
     __shared__ uint32_t scratch[THREADS / 32][8 * kBatchLayoutV * 32];
-    // The A^(2^i) table in shared memory: a block's tiles jump from here
-    // instead of from L2, whose latency a short tile cannot hide.
-    __shared__ __align__(16) uint32_t sjump[kDevJump * 64];
-    for (int q = threadIdx.x; q < kDevJump * 16; q += THREADS)
-        reinterpret_cast<uint4*>(sjump)[q] = reinterpret_cast<const uint4*>(g_jump)[q];
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
     for (;;) {
@@ -110,15 +104,15 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
         uint32_t s[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) s[q] = src[q];
-        warp_jump(sjump, s, in.offset + t.start);
+        warp_jump(g_jwin, s, in.offset + t.start);
         if (t.len_flags & kTileHead) {
             if (lane == 0) {
                 switch (in.kind) {
-                case kU32: run_head<kU32>(in, t, s, sjump); break;
-                case kF64Orig: run_head<kF64Orig>(in, t, s, sjump); break;
-                case kF64Shift: run_head<kF64Shift>(in, t, s, sjump); break;
-                case kF32Orig: run_head<kF32Orig>(in, t, s, sjump); break;
-                default: run_head<kF32Shift>(in, t, s, sjump); break;
+                case kU32: run_head<kU32>(in, t, s, g_jwin); break;
+                case kF64Orig: run_head<kF64Orig>(in, t, s, g_jwin); break;
+                case kF64Shift: run_head<kF64Shift>(in, t, s, g_jwin); break;
+                case kF32Orig: run_head<kF32Orig>(in, t, s, g_jwin); break;
+                default: run_head<kF32Shift>(in, t, s, g_jwin); break;
                 }
             }
             continue;
@@ -151,29 +145,13 @@ __global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ Batch
     }
 }
 
-// Shared memory before L1: the blocks of k_batch hold the jump table.
-static cudaError_t prefer_shared() {
-    static cudaError_t e = [] {
-        cudaError_t r = cudaFuncSetAttribute(k_batch<128>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                             (int)cudaSharedmemCarveoutMaxShared);
-        if (r == cudaSuccess)
-            r = cudaFuncSetAttribute(k_batch<256>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared);
-        return r;
-    }();
-    return e;
-}
-
 cudaError_t launch_batch(const BatchArgs& a, int threads, int blocks, cudaStream_t st) {
-    cudaError_t e = prefer_shared();
-    if (e != cudaSuccess) return e;
     if (threads == 256) k_batch<256><<<blocks, 256, 0, st>>>(a);
     else k_batch<128><<<blocks, 128, 0, st>>>(a);
     return cudaGetLastError();
 }
 
 int batch_blocks_per_sm(int threads) {
-    if (prefer_shared() != cudaSuccess) return 1;
     int nb = 0;
     cudaError_t e = threads == 256
                         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<256>, 256, 0)

@@ -69,11 +69,11 @@ __device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t x) {
 
 // Per-translation-unit device tables and their uploader.
 #define MRG8G_DEFINE_TABLE_UPLOAD(fn_name)                                                      \
-    static __device__ __align__(16) uint32_t g_jump[::mrg8g::kDevJump * 64];                    \
+    static __device__ __align__(16) uint32_t g_jwin[::mrg8g::kJumpWinMats * 64];                \
     static __device__ __align__(16) uint32_t g_win[::mrg8g::kWinWords];                         \
     cudaError_t fn_name() {                                                                    \
         const ::mrg8g::HostTables& t = ::mrg8g::host_tables();                                 \
-        cudaError_t e = cudaMemcpyToSymbol(g_jump, t.jump, sizeof(g_jump));                    \
+        cudaError_t e = cudaMemcpyToSymbol(g_jwin, t.jwin, sizeof(g_jwin));                    \
         if (e != cudaSuccess) return e;                                                        \
         return cudaMemcpyToSymbol(g_win, t.win, sizeof(g_win));                                \
     }
@@ -81,34 +81,37 @@ __device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t x) {
 namespace mrg8g {
 
 // Lane-uniform 8-word state s (canonical or raw words < 2^31) -> A^k s, as
-// canonical residues in [0, p-1], computed by the whole warp: lane l owns
-// row l/4 and columns 2(l%4), 2(l%4)+1 of each A^(2^i) (one 8-byte load),
-// partial sums meet by two xor-shuffles, and the new vector is re-broadcast.
-// Must be called by all 32 lanes with the same s and k.
-__device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jump, uint32_t s[8],
-                                          uint64_t k) {
+// canonical residues in [0, p-1] (k = 0 leaves s as it is), computed by the
+// whole warp from the byte-window table `jwin` (kJumpWinMats matrices
+// A^(j 256^w)): one matrix-vector product per non-zero byte of k, at most
+// eight.  The eight matrices' entries are all requested before the first
+// product, so the jump waits for one table round trip rather than one per
+// step.  Lane l owns row l/4 and columns 2(l%4), 2(l%4)+1 of each matrix (one
+// 8-byte load); partial sums meet by two xor-shuffles and the new vector is
+// re-broadcast.  Must be called by all 32 lanes with the same s and k.
+__device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jwin, uint32_t s[8], uint64_t k) {
     if (k == 0) return;
     const int lane = threadIdx.x & 31;
     const int c0 = (lane & 3) << 1;
+    uint2 m[kJumpBytes];
+#pragma unroll
+    for (int w = 0; w < kJumpBytes; ++w) {
+        const uint32_t j = (uint32_t)(k >> (8 * w)) & 255u;
+        m[w] = j ? __ldg(reinterpret_cast<const uint2*>(jwin + (w * 255 + j - 1) * 64) + lane) : make_uint2(0u, 0u);
+    }
     uint32_t a0 = c0 == 0 ? s[0] : c0 == 2 ? s[2] : c0 == 4 ? s[4] : s[6];
     uint32_t a1 = c0 == 0 ? s[1] : c0 == 2 ? s[3] : c0 == 4 ? s[5] : s[7];
     uint32_t val = 0;
-    // The next matrix's entries are loaded before the current product's
-    // shuffles, so that a load's latency overlaps one step.
-    uint2 m = reinterpret_cast<const uint2*>(jump + (__ffsll((long long)k) - 1) * 64)[lane];
-    for (;;) {
-        k &= k - 1;
-        uint2 mn = make_uint2(0u, 0u);
-        if (k) mn = reinterpret_cast<const uint2*>(jump + (__ffsll((long long)k) - 1) * 64)[lane];
-        const uint64_t part = (uint64_t)m.x * a0 + (uint64_t)m.y * a1;  // < 2^63
-        uint64_t f = (part & kP) + (part >> 31);                        // < 2^33
+#pragma unroll
+    for (int w = 0; w < kJumpBytes; ++w) {
+        if (((k >> (8 * w)) & 255u) == 0) continue;  // lane-uniform
+        const uint64_t part = (uint64_t)m[w].x * a0 + (uint64_t)m[w].y * a1;  // < 2^63
+        uint64_t f = (part & kP) + (part >> 31);                              // < 2^33
         f += __shfl_xor_sync(kFull, f, 1);
-        f += __shfl_xor_sync(kFull, f, 2);                              // < 2^35
+        f += __shfl_xor_sync(kFull, f, 2);                                    // < 2^35
         val = mod_p64(f);
         a0 = __shfl_sync(kFull, val, c0 << 2);
         a1 = __shfl_sync(kFull, val, (c0 << 2) + 4);
-        if (!k) break;
-        m = mn;
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = __shfl_sync(kFull, val, q << 2);

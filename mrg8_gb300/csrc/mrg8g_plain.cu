@@ -5,7 +5,7 @@
 // Replaces rng_outer_32 / rng_inner of cuda/mrg8_cuda.cu:201-399.  Layout of
 // the work: the call's n outputs (stream positions 0..n-1 after the handle's
 // current state) are cut into one contiguous tile per warp.  A warp jumps its
-// state to the tile start with the resident A^(2^i) table, then lane l owns V
+// state to the tile start with the resident byte-window jump table, then lane l owns V
 // interleaved decimated substreams (positions B + V l + v + 32 V j); each is
 // an order-8 recurrence of its own (coefficients of the characteristic
 // polynomial of A^(32V)), so a lane needs 8 multiply-adds per output, no
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kPlainThreads, plain_min_blocks<V, KIND>())
         uint32_t st[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) st[q] = a.st[q];
-        lane_sequential<KIND>(g_jump, st, out, a.head);  // row 0 of A = coefficients
+        lane_sequential<KIND>(g_jwin, st, out, a.head);  // row 0 of A = coefficients
     }
 
     const uint64_t B = a.head + warp * a.tile;
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(kPlainThreads, plain_min_blocks<V, KIND>())
     uint32_t s[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = a.st[q];
-    warp_jump(g_jump, s, B);
+    warp_jump(g_jwin, s, B);
     warp_generate<V, KIND>(g_win, s, out + B, min(a.tile, a.n - B), a.lc, scratch[threadIdx.x >> 5]);
 }
 
@@ -79,14 +79,14 @@ __global__ void __launch_bounds__(kPlainThreads)
         if (k < 8) {
             if (lane == 0) {
                 for (uint64_t i = 0; i < k; ++i) {
-                    const uint32_t S = dot8_ref(g_jump, s);
+                    const uint32_t S = dot8_ref(g_jwin, s);  // row 0 of A
 #pragma unroll
                     for (int q = 7; q > 0; --q) s[q] = s[q - 1];
                     s[0] = S;
                 }
             }
         } else {
-            warp_jump(g_jump, s, k);
+            warp_jump(g_jwin, s, k);
 #pragma unroll
             for (int q = 0; q < 8; ++q) s[q] = rep1p(s[q]);
         }

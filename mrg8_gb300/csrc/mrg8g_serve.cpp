@@ -103,6 +103,7 @@ struct mrg8g_server {
     // statistics
     uint64_t submitted = 0, finished = 0, launches = 0, launched_requests = 0, samples = 0, peak_bytes = 0;
     uint64_t max_inflight = 0, overlapped = 0;
+    uint64_t kernel_ns = 0, kernel_timed = 0;  // device time of stamped launches
     // Kernel intervals of the most recent finished launches (%globaltimer
     // ns), to find launches that ran on the device at the same time.
     struct Interval {
@@ -202,6 +203,8 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
 void note_interval(mrg8g_server* sv, Slot& sl) {
     const unsigned long long a = sl.h_times[0], b = sl.h_times[1];
     if (a == 0 || b < a) return;
+    sv->kernel_ns += b - a;
+    sv->kernel_timed++;
     mrg8g_server::Interval cur{a, b, false};
     for (int i = 0; i < sv->nrecent; ++i) {
         mrg8g_server::Interval& o = sv->recent[i];
@@ -593,6 +596,8 @@ int mrg8g_server_get_stats(mrg8g_server* sv, mrg8g_server_stats* st) {
     st->max_inflight = sv->max_inflight;
     st->overlapped_launches = sv->overlapped;
     st->mean_batch = sv->launches ? (double)sv->launched_requests / (double)sv->launches : 0.0;
+    st->kernel_ns = sv->kernel_ns;
+    st->kernel_launches = sv->kernel_timed;
     return MRG8G_SUCCESS;
 }
 
@@ -712,6 +717,8 @@ int mrg8g_server_loadtest(mrg8g_server* sv, const mrg8g_loadtest_config* cfg, mr
     res->mean_batch = res->launches ? (double)(st.launched_requests - st0.launched_requests) / res->launches : 0;
     res->max_inflight = st.max_inflight;
     res->overlapped_launches = st.overlapped_launches - st0.overlapped_launches;
+    const uint64_t kl = st.kernel_launches - st0.kernel_launches;
+    res->mean_kernel_us = kl ? (double)(st.kernel_ns - st0.kernel_ns) / (double)kl * 1e-3 : 0.0;
     res->peak_bytes = st.peak_bytes;
     res->late_submits = late;
     return MRG8G_SUCCESS;

@@ -129,6 +129,10 @@ static void build(HostTables& t) {
         std::memcpy(t.jump[i], M, sizeof(M));
         matmul_mod(M, M, M);
     }
+    for (int w = 0; w < kJumpBytes; ++w) {
+        std::memcpy(t.jwin[w * 255], t.jump[8 * w], sizeof(M));  // A^(256^w)
+        for (int j = 2; j <= 255; ++j) matmul_mod(t.jwin[w * 255 + j - 2], t.jump[8 * w], t.jwin[w * 255 + j - 1]);
+    }
     // Row vectors u_m = e_0^T A^m, m = 1..1024.
     static uint32_t u[8 * 128 + 1][8];
     for (int c = 0; c < 8; ++c) u[1][c] = kCoef[c];

@@ -17,7 +17,13 @@
 namespace mrg8g {
 
 constexpr int kNumJump = 247;   // A^(2^i), i = 0..246 (jump_matrix.txt depth)
-constexpr int kDevJump = 64;    // powers kept on the device (64-bit offsets)
+
+// Byte-window jump table of the device: jwin[w * 255 + j - 1] = A^(j 256^w)
+// for byte position w = 0..7 and byte value j = 1..255, so a 64-bit jump is
+// at most eight matrix-vector products (one per non-zero byte of the offset)
+// instead of one per set bit.  jwin[0] = A (row 0 = the coefficients).
+constexpr int kJumpBytes = 8;
+constexpr int kJumpWinMats = kJumpBytes * 255;
 
 // Lane layouts of the bulk kernels: a warp of 32 lanes, each lane writing V
 // consecutive outputs per row, so consecutive rows of one lane are d = 32 V
@@ -46,6 +52,8 @@ struct LeapCoef {
 struct HostTables {
     // jump[i][r*8+c] = A^(2^i)(r, c), row-major, canonical residues.
     uint32_t jump[kNumJump][64];
+    // Byte windows (above), row-major like jump: 2040 matrices, 522,240 bytes.
+    uint32_t jwin[kJumpWinMats][64];
     // Window tables, per layout li with stride d: win[off + (o*8 + j)*8 + c]
     // is column c of the row vector e_0^T A^(o + 1 + d j), o in [0, d),
     // j in [0, 8): S[B + o + d j] = win_row . s_B for a state s_B taken at

@@ -16,6 +16,12 @@
 //       reduce_acc, and reduce_acc_alu of the 4-byte kernels) over the whole
 //       stream; writes the row-major jump table to
 //       stdout as raw u32 for the Python side to compare.
+//   check_kernel_math jwin <s0..s7> <k...>
+//       the device jump (warp_jump in mrg8g_device.cuh) emulated lane by lane
+//       on the byte-window table: for each offset k, prints A^k s as
+//       canonical residues, after checking it against jump_matvec (one
+//       product per set bit of k) and every window matrix against
+//       A^(j 256^w) formed from the A^(2^i) table.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -117,13 +123,75 @@ static int leap(const char* path, const uint32_t s0[8]) {
     return bad ? 1 : 0;
 }
 
+// warp_jump of mrg8g_device.cuh, one lane at a time: lane l holds row l/4,
+// columns 2(l%4) and 2(l%4)+1; the four lanes of a row add their folded
+// partial sums (the two xor-shuffles) and reduce with mod_p64.
+static void warp_jump_emulated(const HostTables& t, uint32_t s[8], uint64_t k) {
+    if (k == 0) return;
+    uint32_t v[8];
+    std::memcpy(v, s, sizeof(v));
+    for (int w = 0; w < kJumpBytes; ++w) {
+        const uint32_t j = (uint32_t)(k >> (8 * w)) & 255u;
+        if (!j) continue;
+        const uint32_t* M = t.jwin[w * 255 + j - 1];
+        uint32_t nv[8];
+        for (int r = 0; r < 8; ++r) {
+            uint64_t f = 0;
+            for (int l4 = 0; l4 < 4; ++l4) {
+                const uint64_t part = (uint64_t)M[r * 8 + 2 * l4] * v[2 * l4] + (uint64_t)M[r * 8 + 2 * l4 + 1] * v[2 * l4 + 1];
+                f += (part & kP) + (part >> 31);
+            }
+            nv[r] = mod_p64(f);
+        }
+        std::memcpy(v, nv, sizeof(v));
+    }
+    std::memcpy(s, v, sizeof(v));
+}
+
+static int jwin(const uint32_t s0[8], int nk, char** ks) {
+    const HostTables& t = host_tables();
+    unsigned long bad = 0;
+    for (int w = 0; w < kJumpBytes; ++w) {  // A^(j 256^w) = A^((j-1) 256^w) A^(256^w), independently
+        uint32_t P[64];
+        std::memcpy(P, t.jump[8 * w], sizeof(P));
+        for (int j = 1; j <= 255; ++j) {
+            if (std::memcmp(P, t.jwin[w * 255 + j - 1], sizeof(P))) bad++;
+            // P <- P * A^(256^w) by bits: A^(256^w) = prod of its own square chain
+            uint32_t Q[64];
+            matmul_mod(t.jump[8 * w], P, Q);
+            std::memcpy(P, Q, sizeof(P));
+        }
+    }
+    for (int i = 0; i < nk; ++i) {
+        const uint64_t k = std::strtoull(ks[i], nullptr, 10);
+        uint32_t a[8], b[8];
+        std::memcpy(a, s0, sizeof(a));
+        warp_jump_emulated(t, a, k);
+        jump_matvec(s0, k, b);
+        for (int q = 0; q < 8; ++q) {
+            if (k && a[q] >= kP) bad++;
+            if (a[q] % kP != b[q] % kP) bad++;
+        }
+        std::printf("%llu", (unsigned long long)k);
+        for (int q = 0; q < 8; ++q) std::printf(" %u", a[q]);
+        std::printf("\n");
+    }
+    std::printf("bad=%lu\n", bad);
+    return bad ? 1 : 0;
+}
+
 int main(int argc, char** argv) {
     if (argc >= 2 && !std::strcmp(argv[1], "conv")) return conv();
+    if (argc >= 10 && !std::strcmp(argv[1], "jwin")) {
+        uint32_t s[8];
+        for (int q = 0; q < 8; ++q) s[q] = (uint32_t)std::strtoul(argv[2 + q], nullptr, 10);
+        return jwin(s, argc - 10, argv + 10);
+    }
     if (argc >= 11 && !std::strcmp(argv[1], "leap")) {
         uint32_t s[8];
         for (int q = 0; q < 8; ++q) s[q] = (uint32_t)std::strtoul(argv[3 + q], nullptr, 10);
         return leap(argv[2], s);
     }
-    std::fprintf(stderr, "usage: check_kernel_math conv | leap <stream.bin> s0..s7\n");
+    std::fprintf(stderr, "usage: check_kernel_math conv | leap <stream.bin> s0..s7 | jwin s0..s7 k...\n");
     return 2;
 }

@@ -32,6 +32,40 @@ def test_exports_every_declared_symbol(lib):
     assert lib.mrg8g_version() == 1
 
 
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror in mrg8_gb300/_lib.py has the size and the field
+    offsets that a C compiler gives the struct of include/mrg8g.h."""
+    import subprocess
+
+    from mrg8_gb300 import _lib as L
+    mirrors = {}
+    for name in dir(L):
+        cls = getattr(L, name)
+        if isinstance(cls, type) and issubclass(cls, C.Structure) and cls.__doc__:
+            m = re.match(r"(mrg8g_\w+) of include/mrg8g\.h", cls.__doc__)
+            if m:
+                mirrors[m.group(1)] = cls
+    assert len(mirrors) >= 8, sorted(mirrors)
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "mrg8g.h"', "int main(void) {"]
+    for cname, cls in sorted(mirrors.items()):
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I" + os.path.join(ROOT, "include"), "-o", str(exe), str(src)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
 def test_seeding_and_state(lib, oracle, kat):
     import mrg8_gb300 as m
     for seed, st in kat["seed_states"].items():

@@ -45,3 +45,25 @@ def test_tables_and_decimated_recurrence(native_check, oracle, tmp_path, seed):
     jump = np.frombuffer(r.stdout, dtype=np.uint32).reshape(247, 8, 8)
     tab = oracle.tab.reshape(247, 8, 8).transpose(0, 2, 1)  # column-major -> row-major
     assert np.array_equal(jump, tab)
+
+
+def test_byte_window_jump(native_check, oracle):
+    """The device jump's byte-window table and its lane-by-lane arithmetic
+    (emulated on the host) against the oracle's jump, on offsets with every
+    byte position set and unset, the byte values 1 and 255, and 2^64 - 1."""
+    st = oracle.seed(13579)
+    st[2], st[5] = 0, P  # raw words the device jump accepts
+    rng = np.random.default_rng(3)
+    ks = [0, 1, 7, 8, 255, 256, 257, 65535, 65536, (1 << 64) - 1, 1 << 63, (1 << 56) * 255, 0x0100010001000100]
+    ks += [int(v) for v in rng.integers(0, 1 << 63, 40, dtype=np.int64)]
+    ks += [int(v) >> int(s) for v, s in zip(rng.integers(0, 1 << 63, 20, dtype=np.int64), rng.integers(0, 60, 20))]
+    r = subprocess.run([native_check, "jwin", *[str(int(v)) for v in st], *[str(k) for k in ks]],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr
+    lines = r.stdout.split("\n")
+    assert lines[len(ks)] == "bad=0"
+    for k, line in zip(ks, lines):
+        got = [int(v) for v in line.split()]
+        assert got[0] == k
+        want = oracle.jump(st, k) if k else st
+        assert [g % P for g in got[1:]] == [int(w) % P for w in want], k
