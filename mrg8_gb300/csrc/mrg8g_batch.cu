@@ -3,12 +3,13 @@
 // buffer and output kind).
 //
 // The host cuts every instance into tiles (a short unaligned head tile plus
-// body tiles of a tuned number of rows), longest instances first.  Resident
-// warps pull tile indices from a device counter; each tile jumps the
-// instance's state to the tile's first output with the resident byte-window
-// jump table and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so
-// every instance's values equal its own sequential stream.  This replaces
-// one mrg8_cuda::mrg8_outer_32 launch per instance (cuda/mrg8_cuda.cu:414-436).
+// body tiles of a tuned number of rows), longest instances first.  Each
+// resident warp takes the tile of its own index in the grid, then pulls
+// further tile indices from a device counter; each tile jumps the instance's
+// state to the tile's first output with the resident byte-window jump table
+// and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so every
+// instance's values equal its own sequential stream.  This replaces one
+// mrg8_cuda::mrg8_outer_32 launch per instance (cuda/mrg8_cuda.cu:414-436).
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -28,7 +29,8 @@ __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t
                                          const BatchArgs& a, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     T* out = static_cast<T*>(in.out) + t.start;
-    warp_generate<kBatchLayoutV, KIND>(g_win, s, out, t.len_flags, a.leap[layout_index(kBatchLayoutV)], scratch);
+    warp_generate<kBatchLayoutV, KIND>(g_win, g_dstep, s, out, t.len_flags, a.leap[layout_index(kBatchLayoutV)],
+                                       scratch);
 }
 
 template <int KIND>
@@ -80,15 +82,29 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_batch(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const __grid_constant__ BatchArgs a) {
     if (a.times && blockIdx.x == 0 && threadIdx.x == 0) a.times[0] = global_ns();
-    __shared__ uint32_t scratch[THREADS / 32][8 * kBatchLayoutV * 32];
+    __shared__ __align__(16) uint32_t scratch[THREADS / 32][window_scratch(kBatchLayoutV)];
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
+    // A warp's first tile is its index in the grid; later ones come from the
+    // device counter, offset by the grid's warps, so a launch with no more
+    // tiles than warps never waits on the counter.
+    const uint32_t nwarps = gridDim.x * (THREADS / 32);
+    bool first = true;
     for (;;) {
-        uint32_t ti = 0;
-        if (lane == 0) ti = atomicAdd(a.counter, 1u);
-        ti = __shfl_sync(kFull, ti, 0);
+        uint32_t ti;
+        if (first) {
+            ti = blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
+            first = false;
+        } else {
+            if (a.ntiles <= nwarps) break;
+            uint32_t q = 0;
+            if (lane == 0) q = atomicAdd(a.counter, 1u);
+            const uint64_t next = (uint64_t)nwarps + __shfl_sync(kFull, q, 0);
+            if (next >= a.ntiles) break;
+            ti = (uint32_t)next;
+        }
         if (ti >= a.ntiles) break;
         BatchTile t;
         BatchInst in;

@@ -13,6 +13,9 @@
 namespace mrg8g {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
+// Shared-memory words per warp for lane_window of layout V (the eight
+// states, then the window values of the lane's V substreams).
+MRG8G_HDC constexpr int window_scratch(int V) { return 64 + 8 * V * 32; }
 
 // Output kinds; the numbering is part of the C ABI (include/mrg8g.h).
 enum Kind : int { kU32 = 0, kF64Orig = 1, kF64Shift = 2, kF32Orig = 3, kF32Shift = 4 };
@@ -71,9 +74,12 @@ __device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t x) {
 #define MRG8G_DEFINE_TABLE_UPLOAD(fn_name)                                                      \
     static __device__ __align__(16) uint32_t g_jwin[::mrg8g::kJumpWinMats * 64];                \
     static __device__ __align__(16) uint32_t g_win[::mrg8g::kWinWords];                         \
+    static __device__ __align__(16) uint32_t g_dstep[::mrg8g::kNumLayouts * 7 * 64];            \
     cudaError_t fn_name() {                                                                    \
         const ::mrg8g::HostTables& t = ::mrg8g::host_tables();                                 \
         cudaError_t e = cudaMemcpyToSymbol(g_jwin, t.jwin, sizeof(g_jwin));                    \
+        if (e != cudaSuccess) return e;                                                        \
+        e = cudaMemcpyToSymbol(g_dstep, t.dstep, sizeof(g_dstep));                             \
         if (e != cudaSuccess) return e;                                                        \
         return cudaMemcpyToSymbol(g_win, t.win, sizeof(g_win));                                \
     }
@@ -117,13 +123,6 @@ __device__ __forceinline__ void warp_jump(const uint32_t* __restrict__ jwin, uin
     for (int q = 0; q < 8; ++q) s[q] = __shfl_sync(kFull, val, q << 2);
 }
 
-// Initial window of a lane for layout V: x[v][j] = S[B + o + d j] - 1 with
-// o = sub_offset(lane, v) (V lane + v for the usual layouts)
-// for j = 0..7 (d = 32 V), from the state s taken at stream position B.  The
-// 8 V dot products run four at a time (the four table rows are loaded
-// together, so their latencies overlap, and the setup's register peak stays
-// below the main loop's) through the warp's scratch rows in shared memory,
-// `scratch` holding 8 V * 32 words laid out [slot][lane].
 // Offset within a warp row (32 V outputs) of lane `lane`'s substream v, for
 // outputs of ELEM bytes.  A lane owns V consecutive outputs, except 8-byte
 // outputs with V = 4: there lane l owns the pairs at 2 l and 64 + 2 l, so that
@@ -133,32 +132,76 @@ MRG8G_HDC uint32_t sub_offset(uint32_t lane, uint32_t v) {
     return (ELEM == 8 && V == 4) ? 64u * (v >> 1) + 2u * lane + (v & 1u) : (uint32_t)V * lane + v;
 }
 
+// Initial window of a lane for layout V: x[v][j] = S[B + o + d j] - 1 with
+// o = sub_offset(lane, v) and d = 32 V, for j = 0..7, from the state s taken
+// at stream position B (canonical or raw words < 2^31).  Since
+// S[B + o + d j] = e_0^T A^(o + 1) s_(B + d j) with s_(B + d j) = A^(d j) s,
+// the warp forms the seven states s_(B + d j), j = 1..7 (one warp-cooperative
+// product each, all seven at once, from the `dstep` table) and each lane takes
+// the dot products of its V rows e_0^T A^(o + 1) (row j = 0 of the window
+// table) with the eight states.  The matrices' parts and the first two rows
+// of every lane are requested together, before the first product, so the
+// setup waits for one table round trip after the jump (rows 2 and 3 of V = 4
+// are requested after the products, to keep the register peak below the main
+// loop's).  The states and the finished values pass through the warp's
+// `scratch` (window_scratch(V) words: 64 for the states, then the values
+// laid out [slot][lane]).
 template <int V, int ELEM>
-__device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t s[8],
-                                            int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
-    const uint32_t* w = win + win_offset(layout_index(V));
-#pragma unroll 1
-    for (int i0 = 0; i0 < 8 * V; i0 += 4) {
-        uint4 r[8];
+__device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t* __restrict__ dstep,
+                                            const uint32_t s[8], int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
+    constexpr int li = layout_index(V);
+    constexpr int VE = V < 2 ? V : 2;  // rows requested with the matrices
+    const uint4* rows = reinterpret_cast<const uint4*>(win + win_offset(li));
+    uint4 r[V][2];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int i = i0 + q, v = i >> 3, j = i & 7;
-            const uint4* row = reinterpret_cast<const uint4*>(w + (sub_offset<V, ELEM>(lane, v) * 8 + j) * 8);
-            r[2 * q] = __ldg(row);
-            r[2 * q + 1] = __ldg(row + 1);
-        }
+    for (int v = 0; v < VE; ++v) {
+        r[v][0] = __ldg(rows + sub_offset<V, ELEM>(lane, v) * 16);
+        r[v][1] = __ldg(rows + sub_offset<V, ELEM>(lane, v) * 16 + 1);
+    }
+    uint2 m[7];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const uint4 r0 = r[2 * q], r1 = r[2 * q + 1];
-            const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-            const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
-            scratch[(i0 + q) * 32 + lane] = (S ? S : kP) - 1u;
+    for (int j = 0; j < 7; ++j) m[j] = __ldg(reinterpret_cast<const uint2*>(dstep + (li * 7 + j) * 64) + lane);
+    const int c0 = (lane & 3) << 1;
+    const uint32_t a0 = c0 == 0 ? s[0] : c0 == 2 ? s[2] : c0 == 4 ? s[4] : s[6];
+    const uint32_t a1 = c0 == 0 ? s[1] : c0 == 2 ? s[3] : c0 == 4 ? s[5] : s[7];
+    if (lane == 0) {
+        reinterpret_cast<uint4*>(scratch)[0] = make_uint4(s[0], s[1], s[2], s[3]);
+        reinterpret_cast<uint4*>(scratch)[1] = make_uint4(s[4], s[5], s[6], s[7]);
+    }
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        const uint64_t part = (uint64_t)m[j].x * a0 + (uint64_t)m[j].y * a1;  // < 2^63
+        uint64_t f = (part & kP) + (part >> 31);                              // < 2^33
+        f += __shfl_xor_sync(kFull, f, 1);
+        f += __shfl_xor_sync(kFull, f, 2);                                    // < 2^35
+        if ((lane & 3) == 0) scratch[(j + 1) * 8 + (lane >> 2)] = mod_p64(f);
+    }
+#pragma unroll
+    for (int v = VE; v < V; ++v) {
+        r[v][0] = __ldg(rows + sub_offset<V, ELEM>(lane, v) * 16);
+        r[v][1] = __ldg(rows + sub_offset<V, ELEM>(lane, v) * 16 + 1);
+    }
+    __syncwarp();
+    uint32_t* const xs = scratch + 64;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const uint4 h0 = reinterpret_cast<const uint4*>(scratch + j * 8)[0];
+        const uint4 h1 = reinterpret_cast<const uint4*>(scratch + j * 8)[1];
+        const uint32_t st[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const uint32_t rv[8] = {r[v][0].x, r[v][0].y, r[v][0].z, r[v][0].w,
+                                    r[v][1].x, r[v][1].y, r[v][1].z, r[v][1].w};
+            const uint32_t S = dot8_ref(rv, st);  // [1, p], or 0 for residue 0
+            xs[(v * 8 + j) * 32 + lane] = (S ? S : kP) - 1u;
         }
     }
+    __syncwarp();
 #pragma unroll
     for (int v = 0; v < V; ++v)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[v][j] = scratch[(v * 8 + j) * 32 + lane];
+        for (int j = 0; j < 8; ++j) x[v][j] = xs[(v * 8 + j) * 32 + lane];
+    __syncwarp();  // the scratch words are free again
 }
 
 }  // namespace mrg8g

@@ -73,17 +73,18 @@ __device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const 
 }
 
 // The run of `len` outputs from state s (see the file comment).  `out` must
-// be 16-byte aligned when V > 1; `scratch` is the warp's 8 V * 32-word area.
+// be 16-byte aligned when V > 1; `scratch` is the warp's window_scratch(V)
+// words of shared memory (16-byte aligned).
 template <int V, int KIND>
-__device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, const uint32_t s[8],
-                                              typename OutOf<KIND>::T* out, uint64_t len, const LeapCoef& lc,
-                                              uint32_t* scratch) {
+__device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, const uint32_t* __restrict__ dstep,
+                                              const uint32_t s[8], typename OutOf<KIND>::T* out, uint64_t len,
+                                              const LeapCoef& lc, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     constexpr uint32_t D = 32 * V;
     constexpr bool kAluTail = sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
-    lane_window<V, sizeof(T)>(win, s, lane, scratch, x);
+    lane_window<V, sizeof(T)>(win, dstep, s, lane, scratch, x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
     T* const p = out + sub_offset<V, sizeof(T)>((uint32_t)lane, 0);

@@ -9,7 +9,7 @@
 // interleaved decimated substreams (positions B + V l + v + 32 V j); each is
 // an order-8 recurrence of its own (coefficients of the characteristic
 // polynomial of A^(32V)), so a lane needs 8 multiply-adds per output, no
-// shuffles and no shared memory, and every row j of the warp is one
+// shuffles and no shared memory after its setup, and every row j of the warp is one
 // contiguous 32 V-element run written with 16-byte vector stores.
 #include "mrg8g_device.cuh"
 #include "mrg8g_gen.cuh"
@@ -33,7 +33,7 @@ template <int V, int KIND>
 __global__ void __launch_bounds__(kPlainThreads, plain_min_blocks<V, KIND>())
     k_plain(const __grid_constant__ PlainArgs a) {
     using T = typename OutOf<KIND>::T;
-    __shared__ uint32_t scratch[kPlainThreads / 32][8 * V * 32];
+    __shared__ __align__(16) uint32_t scratch[kPlainThreads / 32][window_scratch(V)];
     T* const out = static_cast<T*>(a.out);
     const int lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kPlainThreads, plain_min_blocks<V, KIND>())
 #pragma unroll
     for (int q = 0; q < 8; ++q) s[q] = a.st[q];
     warp_jump(g_jwin, s, B);
-    warp_generate<V, KIND>(g_win, s, out + B, min(a.tile, a.n - B), a.lc, scratch[threadIdx.x >> 5]);
+    warp_generate<V, KIND>(g_win, g_dstep, s, out + B, min(a.tile, a.n - B), a.lc, scratch[threadIdx.x >> 5]);
 }
 
 // Uniforms from raw stream integers S in [1, p] (grid-stride).

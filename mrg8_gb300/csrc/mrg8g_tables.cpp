@@ -145,8 +145,10 @@ static void build(HostTables& t) {
         for (int o = 0; o < d; ++o)
             for (int j = 0; j < 8; ++j)
                 for (int c = 0; c < 8; ++c) w[(o * 8 + j) * 8 + c] = u[o + 1 + d * j][c];
+        std::memcpy(t.dstep[li][0], t.jump[5 + li], sizeof(M));  // A^d = A^(2^(5+li))
+        for (int j = 2; j <= 7; ++j) matmul_mod(t.dstep[li][j - 2], t.jump[5 + li], t.dstep[li][j - 1]);
         uint32_t beta[8];
-        charpoly_coeffs(t.jump[5 + li], beta);  // A^d = A^(2^(5+li))
+        charpoly_coeffs(t.jump[5 + li], beta);
         t.leap[li] = make_leap(beta);
     }
 }

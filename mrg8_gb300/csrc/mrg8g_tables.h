@@ -59,6 +59,10 @@ struct HostTables {
     // j in [0, 8): S[B + o + d j] = win_row . s_B for a state s_B taken at
     // stream position B.
     uint32_t win[kWinWords];
+    // Row-block steps of the layouts: dstep[li][j - 1] = A^(d j) for
+    // d = layout_stride(li), j = 1..7 (the states at the starts of a warp's
+    // first eight rows, from which its lanes form their windows).
+    uint32_t dstep[kNumLayouts][7][64];
     LeapCoef leap[kNumLayouts];
 };
 

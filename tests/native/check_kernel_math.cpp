@@ -11,7 +11,9 @@
 //       roundings (round-toward-zero fma, round-to-nearest add).
 //   check_kernel_math leap <stream.bin> <s0..s7>
 //       stream.bin holds the oracle's outputs S[0..N) from state s; checks
-//       the window tables (S[B + o + d j] = row . s_B at B = 0) and runs every
+//       the window tables (S[B + o + d j] = row . s_B at B = 0), the kernels'
+//       window setup (row j = 0 against the states A^(d j) s_B formed from
+//       the dstep table with the warp's folded arithmetic), and runs every
 //       layout's decimated recurrence with the kernels' step (mad_wide_s32 +
 //       reduce_acc, and reduce_acc_alu of the 4-byte kernels) over the whole
 //       stream; writes the row-major jump table to
@@ -97,6 +99,21 @@ static int leap(const char* path, const uint32_t s0[8]) {
         const LeapCoef& lc = t.leap[li];
         if (S.size() < (size_t)d * 16) return 3;
         const size_t rows = S.size() / d;
+        // The kernels' lane_window: the states at B + d j from the dstep
+        // table with the warp's folded arithmetic, then row j = 0 of the
+        // window table against each.
+        uint32_t st[8][8];
+        std::memcpy(st[0], s0, sizeof(st[0]));
+        for (int j = 1; j < 8; ++j)
+            for (int r = 0; r < 8; ++r) {
+                uint64_t fsum = 0;
+                for (int l4 = 0; l4 < 4; ++l4) {
+                    const uint32_t* M = t.dstep[li][j - 1];
+                    const uint64_t part = (uint64_t)M[r * 8 + 2 * l4] * s0[2 * l4] + (uint64_t)M[r * 8 + 2 * l4 + 1] * s0[2 * l4 + 1];
+                    fsum += (part & kP) + (part >> 31);
+                }
+                st[j][r] = mod_p64(fsum);
+            }
         for (int o = 0; o < d; ++o) {
             uint32_t x[8];
             for (int j = 0; j < 8; ++j) {
@@ -104,6 +121,10 @@ static int leap(const char* path, const uint32_t s0[8]) {
                 const uint32_t Sv = v ? v : kP;
                 if (Sv != S[o + (size_t)d * j]) bad++;
                 x[j] = Sv - 1u;
+                const uint32_t vd = dot8_ref(w + o * 64, st[j]);
+                if ((vd ? vd : kP) - 1u != x[j]) {
+                    if (bad++ < 8) std::fprintf(stderr, "window mismatch d=%d o=%d j=%d\n", d, o, j);
+                }
             }
             for (size_t j = 8; j < rows; ++j) {
                 uint64_t acc = lc.K1;
