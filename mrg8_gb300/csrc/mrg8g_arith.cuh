@@ -105,6 +105,18 @@ MRG8G_HD uint32_t f32_bits_of(uint32_t v) {
     return bits < xn ? bits : xn;
 }
 
+// ORIGINAL from s = S mod p in [0, p-1] (the lag form of the fp64 ORIGINAL
+// kernels): for s >= 1 the word of f64_bits_below_p (no carry below p), and
+// s = 0 (S = p) gives 1.0, whose low word the same assembly already yields.
+MRG8G_HD uint64_t f64_bits_orig(uint32_t s) {
+    const uint32_t lz = clz32(s);
+    const uint32_t xm = shl_clamp(s, lz) >> 1;
+    const uint32_t t = (xm + 0xFFu + ((xm >> 9) & 1u)) >> 9;
+    const uint32_t lo = (xm << 22) + t;
+    const uint32_t hi = (xm >> 10) - (lz << 20) + (1022u << 20);
+    return ((uint64_t)(s ? hi : 0x3FF00000u) << 32) | lo;
+}
+
 // x is the stream value minus one, 0 <= x <= p - 1 (S = x + 1 in [1, p]).
 MRG8G_HD uint64_t f64_bits(uint32_t x, bool shifted) { return shifted ? f64_bits_below_p(x) : f64_bits_to_p(x + 1u); }
 MRG8G_HD uint32_t f32_bits(uint32_t x, bool shifted) { return f32_bits_of(shifted ? x : x + 1u); }
@@ -186,5 +198,15 @@ MRG8G_HD uint32_t reduce_acc_alu(uint64_t a) {
 
 // Residue in [0, p-1] -> stream representative in [1, p].
 MRG8G_HD uint32_t rep1p(uint32_t r) { return r ? r : kP; }
+
+// Lag forms of the kernels' recurrences, from a dot8_ref result S in [0, p]
+// (0 only for an all-zero sum, i.e. residue 0): x = S - 1 in [0, p-1], or
+// s = S mod p in [0, p-1] for the fp64 ORIGINAL outputs (whose conversion
+// then needs no + 1).
+MRG8G_HD uint32_t lag_minus1(uint32_t S) { return (S ? S : kP) - 1u; }
+MRG8G_HD uint32_t lag_mod(uint32_t S) {
+    const uint32_t z = S - kP;
+    return S < z ? S : z;
+}
 
 }  // namespace mrg8g

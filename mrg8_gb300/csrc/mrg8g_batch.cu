@@ -29,8 +29,7 @@ __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t
                                          const BatchArgs& a, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     T* out = static_cast<T*>(in.out) + t.start;
-    warp_generate<kBatchLayoutV, KIND>(g_win, g_dstep, s, out, t.len_flags, a.leap[layout_index(kBatchLayoutV)],
-                                       scratch);
+    warp_generate<kBatchLayoutV, KIND>(g_win, g_dstep, s, out, t.len_flags, a.leap[kLagMod<KIND> ? 1 : 0], scratch);
 }
 
 template <int KIND>
@@ -325,7 +324,7 @@ extern "C" int mrg8g_batch_generate_noalloc(const mrg8g_instance* inst, uint64_t
     a.tile_elems = 0;
     a.states = nullptr;
     a.times = nullptr;
-    for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+    set_batch_leaps(a);
     const int sms = device_sms();
     const uint64_t want = (ntiles + 3) / 4;
     const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sms * batch_blocks_per_sm(128), want));

@@ -224,7 +224,7 @@ BatchArgs args_of(const mrg8g_batch* b) {
     a.tile_elems = (uint32_t)((uint64_t)b->cfg.tile_rows * 32 * kBatchLayoutV);
     a.states = nullptr;
     a.times = nullptr;
-    for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+    set_batch_leaps(a);
     return a;
 }
 

@@ -161,7 +161,7 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
     a.head = head;
     a.tile = tile;
     a.out = d_out;
-    a.lc = host_tables().leap[li];
+    a.lc = kind == MRG8G_F64_ORIGINAL ? host_tables().leap_mod[li] : host_tables().leap[li];  // kLagMod
     cudaError_t e = launch_plain(kind, V, a, (int)blocks, s);
     if (e != cudaSuccess) return cuda_fail(e, "launching the bulk kernel");
     return MRG8G_SUCCESS;

@@ -58,14 +58,30 @@ __device__ __forceinline__ uint32_t f32_bits_fp(uint32_t v) {
     return v == 0x7FFFFFBFu ? 0x3F800000u : __float_as_uint(f);
 }
 
-// Output word for the stream value S = x + 1 (x in [0, p-1]).
+// fp64 ORIGINAL keeps its lags as S mod p, the other kinds as S - 1
+// (lag_mod / lag_minus1 of mrg8g_arith.cuh, LeapCoef of mrg8g_tables.h):
+// its conversion then needs neither the + 1 nor the carry into the high word
+// (fp64 ORIGINAL at 2^30: 713 -> 747 Goutputs/s).  fp32 ORIGINAL measured
+// slightly slower in that form (834 -> 828, a comparison s - 1 >= 0x7FFFFFBE
+// selecting 1.0 in place of the + 1) and keeps S - 1.
 template <int KIND>
-__device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t x) {
-    if constexpr (KIND == kU32) return x + 1u;
-    else if constexpr (KIND == kF64Orig) return f64_bits(x, false);
-    else if constexpr (KIND == kF64Shift) return f64_bits(x, true);
-    else if constexpr (KIND == kF32Orig) return f32_bits_fp(x + 1u);
-    else return f32_bits_fp(x);
+constexpr bool kLagMod = KIND == kF64Orig;
+
+template <int KIND>
+__device__ __forceinline__ uint32_t lag_of(uint32_t S) {
+    if constexpr (kLagMod<KIND>) return lag_mod(S);
+    else return lag_minus1(S);
+}
+
+// Output word for a lag of the kind's form (S mod p for fp64 ORIGINAL, else
+// S - 1).
+template <int KIND>
+__device__ __forceinline__ typename OutOf<KIND>::T convert(uint32_t lag) {
+    if constexpr (KIND == kU32) return lag + 1u;
+    else if constexpr (KIND == kF64Orig) return f64_bits_orig(lag);
+    else if constexpr (KIND == kF64Shift) return f64_bits(lag, true);
+    else if constexpr (KIND == kF32Orig) return f32_bits_fp(lag + 1u);
+    else return f32_bits_fp(lag);
 }
 
 }  // namespace mrg8g
@@ -132,7 +148,8 @@ MRG8G_HDC uint32_t sub_offset(uint32_t lane, uint32_t v) {
     return (ELEM == 8 && V == 4) ? 64u * (v >> 1) + 2u * lane + (v & 1u) : (uint32_t)V * lane + v;
 }
 
-// Initial window of a lane for layout V: x[v][j] = S[B + o + d j] - 1 with
+// Initial window of a lane for layout V: x[v][j] = the lag (S - 1, or S mod p
+// when LAG_MOD) of S[B + o + d j] with
 // o = sub_offset(lane, v) and d = 32 V, for j = 0..7, from the state s taken
 // at stream position B (canonical or raw words < 2^31).  Since
 // S[B + o + d j] = e_0^T A^(o + 1) s_(B + d j) with s_(B + d j) = A^(d j) s,
@@ -146,7 +163,7 @@ MRG8G_HDC uint32_t sub_offset(uint32_t lane, uint32_t v) {
 // loop's).  The states and the finished values pass through the warp's
 // `scratch` (window_scratch(V) words: 64 for the states, then the values
 // laid out [slot][lane]).
-template <int V, int ELEM>
+template <int V, int ELEM, bool LAG_MOD>
 __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, const uint32_t* __restrict__ dstep,
                                             const uint32_t s[8], int lane, uint32_t* scratch, uint32_t (&x)[V][8]) {
     constexpr int li = layout_index(V);
@@ -193,7 +210,7 @@ __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, co
             const uint32_t rv[8] = {r[v][0].x, r[v][0].y, r[v][0].z, r[v][0].w,
                                     r[v][1].x, r[v][1].y, r[v][1].z, r[v][1].w};
             const uint32_t S = dot8_ref(rv, st);  // [1, p], or 0 for residue 0
-            xs[(v * 8 + j) * 32 + lane] = (S ? S : kP) - 1u;
+            xs[(v * 8 + j) * 32 + lane] = LAG_MOD ? lag_mod(S) : lag_minus1(S);
         }
     }
     __syncwarp();

@@ -84,7 +84,7 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
     constexpr bool kAluTail = sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
-    lane_window<V, sizeof(T)>(win, dstep, s, lane, scratch, x);
+    lane_window<V, sizeof(T), kLagMod<KIND>>(win, dstep, s, lane, scratch, x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
     T* const p = out + sub_offset<V, sizeof(T)>((uint32_t)lane, 0);
@@ -120,7 +120,7 @@ __device__ __forceinline__ void lane_sequential(const uint32_t* __restrict__ coe
 #pragma unroll
         for (int q = 7; q > 0; --q) st[q] = st[q - 1];
         st[0] = S;
-        out[i] = convert<KIND>(S - 1u);
+        out[i] = convert<KIND>(lag_of<KIND>(S));
     }
 }
 

@@ -68,7 +68,7 @@ struct BatchArgs {
     unsigned long long* times;  // null, or [start, end] of the launch in
                                 // %globaltimer ns (block 0's start, the last
                                 // block's end), written for the serving stats
-    LeapCoef leap[kNumLayouts];
+    LeapCoef leap[2];  // the batch layout's recurrence: [0] lags S - 1, [1] lags S mod p
 };
 
 cudaError_t upload_tables_plain();

@@ -61,7 +61,7 @@ __global__ void k_convert(const uint32_t* __restrict__ in, typename OutOf<KIND>:
                           uint64_t n) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)
-        out[i] = convert<KIND>(in[i] - 1u);
+        out[i] = convert<KIND>(lag_of<KIND>(in[i]));
 }
 
 // states[8 i .. 8 i + 7] = A^offsets[i] st, one warp per offset.  Offsets

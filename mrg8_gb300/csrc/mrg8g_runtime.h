@@ -28,6 +28,12 @@ int default_layout_V(int kind);
 // keeps its register count (one kernel holds the code of all five kinds) low
 // enough for eight resident blocks of 128 threads per SM.
 constexpr int kBatchLayoutV = 2;
+
+// BatchArgs::leap for the batch layout (both lag forms).
+inline void set_batch_leaps(BatchArgs& a) {
+    a.leap[0] = host_tables().leap[layout_index(kBatchLayoutV)];
+    a.leap[1] = host_tables().leap_mod[layout_index(kBatchLayoutV)];
+}
 int validate_state(const uint32_t st[8]);
 void advance_state(uint32_t st[8], uint64_t n);
 int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, cudaStream_t s, int V);

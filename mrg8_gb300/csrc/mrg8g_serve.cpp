@@ -184,7 +184,7 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
         a.done_blocks = sl.d_counter + 1;  // the kernel leaves both at zero
         a.states = sv->d_states;
         a.times = sl.d_times;
-        for (int li = 0; li < kNumLayouts; ++li) a.leap[li] = host_tables().leap[li];
+        set_batch_leaps(a);
         const uint64_t wpb = (uint64_t)sv->cfg.threads / 32;
         const uint64_t want = (ntiles + wpb - 1) / wpb;
         const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)sv->sms * sv->bps, want));

@@ -97,7 +97,9 @@ static void charpoly_coeffs(const uint32_t* M, uint32_t beta[8]) {
     }
 }
 
-static LeapCoef make_leap(const uint32_t beta[8]) {
+// K1 == sum_k c_k - 1 (mod p) for lags x = S - 1, K1 == 0 (mod p) for lags
+// s = S mod p (mod_lags).
+static LeapCoef make_leap(const uint32_t beta[8], bool mod_lags) {
     LeapCoef lc;
     int64_t csum = 0;
     unsigned __int128 negsum = 0, possum = 0;
@@ -108,9 +110,9 @@ static LeapCoef make_leap(const uint32_t beta[8]) {
         if (c < 0) negsum += (unsigned __int128)(-c);
         else possum += (unsigned __int128)c;
     }
-    // K1 == sum c_k - 1 (mod p), the smallest such value >= negsum (p - 1), so
-    // that K1 + sum c_k x_k (x_k in [0, p-1]) stays in [0, 2^64 - 1).
-    const uint64_t cmod = (uint64_t)(((csum - 1) % (int64_t)kP + (int64_t)kP) % (int64_t)kP);
+    // K1 == cmod (mod p), the smallest such value >= negsum (p - 1), so that
+    // K1 + sum c_k x_k (x_k in [0, p-1]) stays in [0, 2^64 - 1).
+    const uint64_t cmod = mod_lags ? 0 : (uint64_t)(((csum - 1) % (int64_t)kP + (int64_t)kP) % (int64_t)kP);
     const unsigned __int128 base = negsum * (kP - 1);
     const uint64_t bmod = (uint64_t)(base % kP);
     const unsigned __int128 K1 = base + (cmod + kP - bmod) % kP;
@@ -149,7 +151,8 @@ static void build(HostTables& t) {
         for (int j = 2; j <= 7; ++j) matmul_mod(t.dstep[li][j - 2], t.jump[5 + li], t.dstep[li][j - 1]);
         uint32_t beta[8];
         charpoly_coeffs(t.jump[5 + li], beta);
-        t.leap[li] = make_leap(beta);
+        t.leap[li] = make_leap(beta, false);
+        t.leap_mod[li] = make_leap(beta, true);
     }
 }
 

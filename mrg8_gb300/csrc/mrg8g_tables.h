@@ -40,10 +40,12 @@ constexpr int kWinWords = (32 + 64 + 128) * 64;
 // x^8 - sum beta_k x^(8-k) is the characteristic polynomial of A^d
 // (Cayley-Hamilton).  For the kernels the coefficients are stored signed,
 // c_k = beta_k or beta_k - p (|c_k| < 2^30), and the kernels keep the lagged
-// values as x = S - 1 in [0, p-1]; then
+// values as x = S - 1 in [0, p-1] (`leap`); then
 //     a = K1 + sum_k c_k x_{j-k}
 // lies in [0, 2^64 - 1) and a == S_j - 1 (mod p), where K1 == sum_k c_k - 1
-// (mod p) is the smallest such constant keeping a >= 0.
+// (mod p) is the smallest such constant keeping a >= 0.  With the lagged
+// values kept as s = S mod p instead (`leap_mod`, the fp64 ORIGINAL outputs), the
+// same coefficients and K1 == 0 (mod p) give a == S_j (mod p).
 struct LeapCoef {
     int32_t c[8];
     uint64_t K1;
@@ -64,6 +66,7 @@ struct HostTables {
     // first eight rows, from which its lanes form their windows).
     uint32_t dstep[kNumLayouts][7][64];
     LeapCoef leap[kNumLayouts];
+    LeapCoef leap_mod[kNumLayouts];
 };
 
 // Built once (thread-safe) on first use.

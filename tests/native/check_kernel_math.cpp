@@ -8,7 +8,8 @@
 //       (1.0/(2^31-1))) and (float) of it; plus the SHIFTED zero.  Also the
 //       fp32 word of the kernels' FP32-pipe form (f32_bits_fp in
 //       mrg8g_device.cuh), through an exact integer emulation of its two
-//       roundings (round-toward-zero fma, round-to-nearest add).
+//       roundings (round-toward-zero fma, round-to-nearest add); and the
+//       fp64 ORIGINAL form that takes s = S mod p (f64_bits_orig).
 //   check_kernel_math leap <stream.bin> <s0..s7>
 //       stream.bin holds the oracle's outputs S[0..N) from state s; checks
 //       the window tables (S[B + o + d j] = row . s_B at B = 0), the kernels'
@@ -39,8 +40,7 @@ static int bitlen(uint64_t x) { return x ? 64 - __builtin_clzll(x) : 0; }
 // Float bits of f32_bits_fp(v): fh = vh 2^-15 and fl = vl 2^-31 are exact;
 // c = RZ(fh 2^-31 + fl) and f = RN(fh + c) are emulated on integers in
 // units of 2^-46 (both operands are exact multiples of it).
-static uint32_t f32_fp_emulated(uint32_t v) {
-    if (v == 0x7FFFFFBFu) return 0x3F800000u;
+static uint32_t f32_fp_core(uint32_t v) {
     const uint64_t vh = v >> 16, vl = v & 0xFFFFu;
     uint64_t c = (vl << 15) + vh;  // (vl + vh 2^-15) 2^-31 in units of 2^-46
     int nb = bitlen(c);
@@ -59,6 +59,7 @@ static uint32_t f32_fp_emulated(uint32_t v) {
     std::memcpy(&b, &f, 4);
     return b;
 }
+static uint32_t f32_fp_emulated(uint32_t v) { return v == 0x7FFFFFBFu ? 0x3F800000u : f32_fp_core(v); }
 
 static int conv() {
     const double rnorm = 1.0 / 2147483647.0;
@@ -77,6 +78,11 @@ static int conv() {
         if (v < 2147483647ull && (f64_bits((uint32_t)v, true) != db || f32_bits((uint32_t)v, true) != fb))
             bad++;
         if (f64_bits((uint32_t)v - 1, false) != db || f32_bits((uint32_t)v - 1, false) != fb) bad++;
+        // The fp64 ORIGINAL kernels convert s = S mod p (S = p -> s = 0).
+        const uint32_t s = (uint32_t)(v % 2147483647ull);
+        if (f64_bits_orig(s) != db) {
+            if (bad++ < 8) std::fprintf(stderr, "ORIGINAL lag-form mismatch at v=%lu\n", (unsigned long)v);
+        }
     }
     if (f64_bits(0, true) != 0 || f32_bits(0, true) != 0 || f32_fp_emulated(0) != 0) bad++;
     std::printf("conv bad=%lu\n", bad);
@@ -126,13 +132,20 @@ static int leap(const char* path, const uint32_t s0[8]) {
                     if (bad++ < 8) std::fprintf(stderr, "window mismatch d=%d o=%d j=%d\n", d, o, j);
                 }
             }
+            uint32_t sm[8];  // the same substream with lags S mod p (fp64 ORIGINAL kernels)
+            for (int j = 0; j < 8; ++j) sm[j] = lag_mod(x[j] + 1u);
+            const LeapCoef& lm = t.leap_mod[li];
             for (size_t j = 8; j < rows; ++j) {
-                uint64_t acc = lc.K1;
-                for (int k = 1; k <= 8; ++k) acc = mad_wide_s32(lc.c[k - 1], x[(j - k) & 7], acc);
+                uint64_t acc = lc.K1, accm = lm.K1;
+                for (int k = 1; k <= 8; ++k) {
+                    acc = mad_wide_s32(lc.c[k - 1], x[(j - k) & 7], acc);
+                    accm = mad_wide_s32(lm.c[k - 1], sm[(j - k) & 7], accm);
+                }
                 const uint32_t xn = reduce_acc(acc);
                 if (reduce_acc_alu(acc) != xn) bad++;
                 x[j & 7] = xn;
-                if (xn + 1u != S[o + (size_t)d * j]) {
+                sm[j & 7] = reduce_acc(accm);
+                if (xn + 1u != S[o + (size_t)d * j] || sm[j & 7] != S[o + (size_t)d * j] % kP) {
                     if (bad++ < 8) std::fprintf(stderr, "leap mismatch d=%d o=%d j=%zu\n", d, o, j);
                 }
                 checked++;
