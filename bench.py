@@ -9,6 +9,8 @@ output (8 GiB) is larger than L2, so no flush is needed between steps.
   e2e      the same through the C ABI with a pinned HOST buffer
            (mrg8g_generate_host: device staging + D2H inside the timed region)
   roofline HBM-write roofline of the bulk kernel against MEASURED_PEAKS.json
+  f32      fp32 SHIFTED at the same size, and (other_kinds) uint32, fp64
+           ORIGINAL and fp32 ORIGINAL
   cpu_baseline  the reference's CPU paths on the host: the block-split
            generator on all cores (knl/mrg8_vec.h:500-525) and the scalar
            sequential rand() of original/mrg8.cpp:231-239 on one core,
@@ -587,6 +589,26 @@ def run_gpu(args) -> None:
         del out32
         f32 = {"value": round(n / f32_s / 1e9, 4), "unit": UNIT, "gbs": round(4.0 * n / f32_s / 1e9, 1),
                "frac_hbm": round(4.0 * n / f32_s / 1e9 / hbm, 4)}
+        # The remaining output kinds at the same size (line items).
+        from mrg8_gb300 import _lib as L
+        buf = torch.empty(n * 8, dtype=torch.uint8, device=dev)
+        f32["other_kinds"] = {}
+        for name, kd, dt, eb in (("u32", L.U32, torch.int32, 4), ("f64_original", L.F64_ORIGINAL, torch.float64, 8),
+                                 ("f32_original", L.F32_ORIGINAL, torch.float32, 4)):
+            view = buf.view(dt)[:n]
+            for _ in range(3):
+                g.set_state(st0)
+                g._generate(view, n, kd)
+            e0.record(stream)
+            for _ in range(reps):
+                g.set_state(st0)
+                g._generate(view, n, kd)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ks = e0.elapsed_time(e1) / 1e3 / reps
+            f32["other_kinds"][name] = {"value": round(n / ks / 1e9, 4), "gbs": round(eb * n / ks / 1e9, 1),
+                                        "frac_hbm": round(eb * n / ks / 1e9 / hbm, 4)}
+        del buf
 
     # End to end through the C ABI with a pinned host buffer.
     e2e = None
