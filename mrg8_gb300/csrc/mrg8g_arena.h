@@ -4,68 +4,76 @@
 // (tests/native/check_arena.cpp).
 #pragma once
 #include <cstdint>
-#include <deque>
+#include <iterator>
+#include <map>
+#include <unordered_map>
 
 namespace mrg8g {
 
-// First-in first-out arena over [0, cap): blocks are handed out in admission
-// order and reclaimed from the oldest once released (out-of-order releases
-// wait for the older ones).  256-byte granularity.  Every block (and every
-// padding block left at the end when the ring wraps) gets the next sequence
-// number, so a release finds its block in O(1).
+// First-fit arena over [0, cap) at 256-byte granularity.  Free space is kept
+// as address-ordered ranges that are merged with their neighbours on release,
+// so a request fits whenever some free range is large enough, whatever order
+// the results are released in.  (A first-in first-out ring cannot reuse the
+// space of a released block while an older one is still held; a client that
+// kept its oldest result while waiting for newer ones could then wait
+// forever.)  Every block gets a fresh sequence number, its release handle, so
+// a repeated or stale release is ignored.
 class Arena {
 public:
-    explicit Arena(uint64_t cap) : cap_(cap) {}
+    explicit Arena(uint64_t cap) : cap_(cap) {
+        if (cap_) free_[0] = cap_;
+    }
     bool alloc(uint64_t bytes, uint64_t* off, uint64_t* seq) {
         bytes = bytes ? (bytes + 255) / 256 * 256 : 256;
         if (bytes > cap_) return false;
-        if (blocks_.empty()) head_ = tail_ = 0;
-        // Live blocks occupy [tail, head) or, once wrapped, [tail, cap) + [0, head).
-        const bool wrapped = !blocks_.empty() && head_ <= tail_;
-        uint64_t at;
-        if (!wrapped) {
-            if (cap_ - head_ >= bytes) {
-                at = head_;
-            } else if (tail_ >= bytes) {
-                if (head_ < cap_) blocks_.push_back({head_, cap_ - head_, true});  // unused end
-                at = 0;
-            } else {
-                return false;
-            }
-        } else if (tail_ - head_ >= bytes) {
-            at = head_;
-        } else {
-            return false;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes) continue;
+            const uint64_t at = it->first, rest = it->second - bytes;
+            free_.erase(it);
+            if (rest) free_[at + bytes] = rest;
+            *off = at;
+            *seq = next_seq_++;
+            live_[*seq] = Block{at, bytes};
+            used_ += bytes;
+            return true;
         }
-        *seq = base_seq_ + blocks_.size();
-        blocks_.push_back({at, bytes, false});
-        head_ = at + bytes;
-        used_ += bytes;
-        *off = at;
-        return true;
+        return false;
     }
     void release(uint64_t seq) {
-        if (seq < base_seq_ || seq - base_seq_ >= blocks_.size()) return;
-        Block& b = blocks_[seq - base_seq_];
-        if (b.released) return;
-        b.released = true;
-        used_ -= b.size;
-        while (!blocks_.empty() && blocks_.front().released) {
-            blocks_.pop_front();
-            ++base_seq_;
+        auto it = live_.find(seq);
+        if (it == live_.end()) return;
+        uint64_t at = it->second.off, size = it->second.size;
+        live_.erase(it);
+        used_ -= size;
+        auto next = free_.lower_bound(at);
+        if (next != free_.end() && at + size == next->first) {
+            size += next->second;
+            next = free_.erase(next);
         }
-        if (blocks_.empty()) head_ = tail_ = 0;
-        else tail_ = blocks_.front().off;
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == at) {
+                prev->second += size;
+                return;
+            }
+        }
+        free_[at] = size;
     }
     uint64_t used() const { return used_; }
+    // Largest free range (for tests and diagnostics).
+    uint64_t largest_free() const {
+        uint64_t m = 0;
+        for (const auto& f : free_) m = f.second > m ? f.second : m;
+        return m;
+    }
 
 private:
     struct Block {
         uint64_t off, size;
-        bool released;
     };
-    uint64_t cap_, head_ = 0, tail_ = 0, used_ = 0, base_seq_ = 0;
-    std::deque<Block> blocks_;
+    uint64_t cap_, used_ = 0, next_seq_ = 0;
+    std::map<uint64_t, uint64_t> free_;           // offset -> length
+    std::unordered_map<uint64_t, Block> live_;    // sequence number -> block
 };
 
 }  // namespace mrg8g

@@ -122,7 +122,7 @@ int normalise(mrg8g_batch_config& c) {
 int upload_insts(mrg8g_batch* b, const BatchInst* src, bool sorted) {
     cudaError_t e;
     if (!b->insts.empty() &&
-        (e = cudaMemcpy(b->d_insts, src, b->insts.size() * sizeof(BatchInst), cudaMemcpyHostToDevice)) != cudaSuccess)
+        (e = copy_to_device(b->d_insts, src, b->insts.size() * sizeof(BatchInst))) != cudaSuccess)
         return cuda_fail(e, "cudaMemcpy(instances)");
     b->d_insts_sorted = sorted;
     return MRG8G_SUCCESS;
@@ -139,7 +139,7 @@ int plan_derived(mrg8g_batch* b) {
     cudaError_t e;
     if (!b->d_base && (e = cudaMalloc(&b->d_base, base.size() * sizeof(uint32_t))) != cudaSuccess)
         return cuda_fail(e, "cudaMalloc(tile counts)");
-    if ((e = cudaMemcpy(b->d_base, base.data(), base.size() * sizeof(uint32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = copy_to_device(b->d_base, base.data(), base.size() * sizeof(uint32_t))) != cudaSuccess)
         return cuda_fail(e, "cudaMemcpy(tile counts)");
     int rc = upload_insts(b, sorted.data(), true);
     if (rc) return rc;
@@ -162,8 +162,7 @@ int upload_tiles(mrg8g_batch* b) {
         b->d_tiles_cap = need;
     }
     if (!b->tiles.empty() &&
-        (e = cudaMemcpy(b->d_tiles, b->tiles.data(), b->tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice)) !=
-            cudaSuccess)
+        (e = copy_to_device(b->d_tiles, b->tiles.data(), b->tiles.size() * sizeof(BatchTile))) != cudaSuccess)
         return cuda_fail(e, "cudaMemcpy(tiles)");
     return MRG8G_SUCCESS;
 }
@@ -331,8 +330,7 @@ static int batch_create(const mrg8g_instance* inst, uint64_t count, const mrg8g_
         destroy_plan(b);
         return cuda_fail(e, "cudaMalloc(batch)");
     }
-    if (count && (e = cudaMemcpy(b->d_insts, b->insts.data(), count * sizeof(BatchInst), cudaMemcpyHostToDevice)) !=
-                     cudaSuccess) {
+    if (count && (e = copy_to_device(b->d_insts, b->insts.data(), count * sizeof(BatchInst))) != cudaSuccess) {
         destroy_plan(b);
         return cuda_fail(e, "cudaMemcpy(instances)");
     }

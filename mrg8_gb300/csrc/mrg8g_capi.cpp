@@ -73,6 +73,11 @@ int ensure_device(int* dev_out, const DeviceInfo** info) {
         if (e != cudaSuccess) return cuda_fail(e, "uploading the jump tables");
         e = upload_tables_batch();
         if (e != cudaSuccess) return cuda_fail(e, "uploading the jump tables (batch)");
+        // The uploads come from pageable memory on the legacy default stream:
+        // wait until they have landed, since kernels on non-blocking streams
+        // are not ordered after them.
+        e = cudaStreamSynchronize(0);
+        if (e != cudaSuccess) return cuda_fail(e, "uploading the jump tables (wait)");
         for (int k = 0; k < 5; ++k)
             for (int li = 0; li < kNumLayouts; ++li) d.bps[k][li] = plain_blocks_per_sm(k, 1 << li);
         d.ready = true;

@@ -34,6 +34,16 @@ inline void set_batch_leaps(BatchArgs& a) {
     a.leap[0] = host_tables().leap[layout_index(kBatchLayoutV)];
     a.leap[1] = host_tables().leap_mod[layout_index(kBatchLayoutV)];
 }
+// Host -> device copy from pageable memory that has reached the device when
+// it returns.  A plain cudaMemcpy from pageable memory may return once the
+// data is staged, before the copy lands, and nothing orders that copy (on the
+// legacy default stream) before work on a non-blocking stream, such as the
+// serving slots or a caller's stream.
+inline cudaError_t copy_to_device(void* dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(0);
+}
+
 int validate_state(const uint32_t st[8]);
 void advance_state(uint32_t st[8], uint64_t n);
 int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, cudaStream_t s, int V);

@@ -422,7 +422,7 @@ int mrg8g_server_create(const mrg8g_server_config* cfg, mrg8g_server** out) {
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaMalloc(&sl.d_stage, stage)) != cudaSuccess ||
             (e = cudaMalloc(&sl.d_counter, 2 * sizeof(uint32_t))) != cudaSuccess ||
-            (e = cudaMemset(sl.d_counter, 0, 2 * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMemsetAsync(sl.d_counter, 0, 2 * sizeof(uint32_t), sl.stream)) != cudaSuccess ||
             (e = cudaHostAlloc(&sl.h_stage, stage, cudaHostAllocDefault)) != cudaSuccess ||
             (e = cudaEventCreateWithFlags(&sl.done_ev, cudaEventDisableTiming)) != cudaSuccess) {
             destroy_server(sv);
@@ -457,7 +457,7 @@ int mrg8g_server_add_generator(mrg8g_server* sv, const uint32_t state[8], uint32
     std::lock_guard<std::mutex> lk(sv->mu);
     if (sv->gen_pos.size() >= sv->cfg.max_generators) return fail(MRG8G_ERR_BUDGET, "generator table is full");
     const uint32_t k = (uint32_t)sv->gen_pos.size();
-    cudaError_t e = cudaMemcpy(sv->d_states + 8ull * k, state, 8 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    cudaError_t e = copy_to_device(sv->d_states + 8ull * k, state, 8 * sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_fail(e, "serving: generator upload");
     std::array<uint32_t, 8> st;
     std::memcpy(st.data(), state, sizeof(uint32_t) * 8);

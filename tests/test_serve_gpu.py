@@ -129,11 +129,41 @@ def test_admission_respects_the_budget(cuda, oracle):
             assert st["bytes_in_use"] <= budget
             while len(held) > 1:
                 srv.release(held.pop(0))
+        st = srv.stats()
+        assert len(results) == len(ts), (st, sorted(results))
         for h in held:
             srv.release(h)
         assert srv.stats()["peak_bytes"] <= budget
     for s, t in enumerate(ts):
         assert np.array_equal(results[t].view(np.uint64), segment(oracle, s, s, n, po.F64_SHIFTED).view(np.uint64))
+
+
+def test_space_released_behind_a_held_result_is_reused(cuda, oracle):
+    """Two results fit in the arena.  The client keeps the older one and
+    releases the newer; the next request must fit into the released space
+    and complete (a ring arena would wait for the older one forever)."""
+    from mrg8_gb300.serve import Server
+    budget = 4 << 20
+    n = (budget // 8) // 3
+    with Server(budget_bytes=budget, inflight=2) as srv:
+        first = [srv.submit(n, po.F64_SHIFTED, seed=s, offset=s) for s in range(2)]
+        got = {}
+        deadline = time.time() + 20
+        while len(got) < 2 and time.time() < deadline:
+            for c in srv.poll(4, 2000):
+                got[c["ticket"]] = c
+        assert sorted(got) == sorted(first)
+        srv.release(first[1])           # the newer one; the older stays held
+        nxt = srv.submit(n, po.F64_SHIFTED, seed=2, offset=2)
+        done = []
+        deadline = time.time() + 20
+        while not done and time.time() < deadline:
+            done = srv.poll(4, 2000)
+        assert [c["ticket"] for c in done] == [nxt], srv.stats()
+        out = srv.read(done[0])
+        srv.release(nxt)
+        srv.release(first[0])
+    assert np.array_equal(out.view(np.uint64), segment(oracle, 2, 2, n, po.F64_SHIFTED).view(np.uint64))
 
 
 def test_loadtest_smoke(cuda):
