@@ -3,9 +3,9 @@
 // buffer and output kind).
 //
 // The host cuts every instance into tiles (a short unaligned head tile plus
-// body tiles of a tuned number of rows), longest instances first.  Each
-// resident warp takes the tile of its own index in the grid, then pulls
-// further tile indices from a device counter; each tile jumps the instance's
+// body tiles of a tuned number of rows), longest instances first.  Resident
+// warps pull tile indices from a device counter (or, in a launch with no more
+// tiles than warps, take the tile of their own index); each tile jumps the instance's
 // state to the tile's first output with the resident byte-window jump table
 // and runs the same warp routine as the bulk kernel (mrg8g_gen.cuh), so every
 // instance's values equal its own sequential stream.  This replaces one
@@ -24,12 +24,13 @@ namespace mrg8g {
 
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_batch)
 
-template <int KIND>
+template <int KIND, bool QUICK>
 __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t, const uint32_t s[8],
                                          const BatchArgs& a, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     T* out = static_cast<T*>(in.out) + t.start;
-    warp_generate<kBatchLayoutV, KIND>(g_win, g_dstep, s, out, t.len_flags, a.leap[kLagMod<KIND> ? 1 : 0], scratch);
+    warp_generate<kBatchLayoutV, KIND, QUICK>(g_win, g_dstep, s, out, t.len_flags, a.leap[kLagMod<KIND> ? 1 : 0],
+                                              scratch);
 }
 
 template <int KIND>
@@ -80,29 +81,28 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-template <int THREADS>
+// QUICK: a launch with no more tiles than warps (launch_batch decides), whose
+// time is its latency: each warp takes the tile of its own index in the grid
+// (no wait on the counter) and forms its window in one table round trip.
+// Otherwise warps pull tiles from the counter and use the row-table window,
+// the faster form when the setup's latency hides behind other warps' work
+// (10,000 uneven instances: 896 Goutputs/s against 876 with the QUICK forms).
+template <int THREADS, bool QUICK>
 __global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const __grid_constant__ BatchArgs a) {
     if (a.times && blockIdx.x == 0 && threadIdx.x == 0) a.times[0] = global_ns();
-    __shared__ __align__(16) uint32_t scratch[THREADS / 32][window_scratch(kBatchLayoutV)];
+    __shared__ __align__(16) uint32_t
+        scratch[THREADS / 32][QUICK ? window_scratch(kBatchLayoutV) : window_rows_scratch(kBatchLayoutV)];
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
-    // A warp's first tile is its index in the grid; later ones come from the
-    // device counter, offset by the grid's warps, so a launch with no more
-    // tiles than warps never waits on the counter.
-    const uint32_t nwarps = gridDim.x * (THREADS / 32);
-    bool first = true;
-    for (;;) {
+    for (int round = 0;; ++round) {
         uint32_t ti;
-        if (first) {
+        if constexpr (QUICK) {
+            if (round) break;
             ti = blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
-            first = false;
         } else {
-            if (a.ntiles <= nwarps) break;
             uint32_t q = 0;
             if (lane == 0) q = atomicAdd(a.counter, 1u);
-            const uint64_t next = (uint64_t)nwarps + __shfl_sync(kFull, q, 0);
-            if (next >= a.ntiles) break;
-            ti = (uint32_t)next;
+            ti = __shfl_sync(kFull, q, 0);
         }
         if (ti >= a.ntiles) break;
         BatchTile t;
@@ -133,11 +133,11 @@ __global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const
             continue;
         }
         switch (in.kind) {
-        case kU32: run_tile<kU32>(in, t, s, a, sc); break;
-        case kF64Orig: run_tile<kF64Orig>(in, t, s, a, sc); break;
-        case kF64Shift: run_tile<kF64Shift>(in, t, s, a, sc); break;
-        case kF32Orig: run_tile<kF32Orig>(in, t, s, a, sc); break;
-        default: run_tile<kF32Shift>(in, t, s, a, sc); break;
+        case kU32: run_tile<kU32, QUICK>(in, t, s, a, sc); break;
+        case kF64Orig: run_tile<kF64Orig, QUICK>(in, t, s, a, sc); break;
+        case kF64Shift: run_tile<kF64Shift, QUICK>(in, t, s, a, sc); break;
+        case kF32Orig: run_tile<kF32Orig, QUICK>(in, t, s, a, sc); break;
+        default: run_tile<kF32Shift, QUICK>(in, t, s, a, sc); break;
         }
     }
     // Self-resetting queue: once every block has left the loop, no warp
@@ -161,16 +161,22 @@ __global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const
 }
 
 cudaError_t launch_batch(const BatchArgs& a, int threads, int blocks, cudaStream_t st) {
-    if (threads == 256) k_batch<256><<<blocks, 256, 0, st>>>(a);
-    else k_batch<128><<<blocks, 128, 0, st>>>(a);
+    const bool quick = (uint64_t)a.ntiles <= (uint64_t)blocks * (uint64_t)(threads / 32);
+    if (threads == 256) {
+        if (quick) k_batch<256, true><<<blocks, 256, 0, st>>>(a);
+        else k_batch<256, false><<<blocks, 256, 0, st>>>(a);
+    } else {
+        if (quick) k_batch<128, true><<<blocks, 128, 0, st>>>(a);
+        else k_batch<128, false><<<blocks, 128, 0, st>>>(a);
+    }
     return cudaGetLastError();
 }
 
 int batch_blocks_per_sm(int threads) {
     int nb = 0;
     cudaError_t e = threads == 256
-                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<256>, 256, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<128>, 128, 0);
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<256, false>, 256, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<128, false>, 128, 0);
     if (e != cudaSuccess || nb <= 0) return 1;
     return nb;
 }

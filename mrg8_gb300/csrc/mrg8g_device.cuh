@@ -14,8 +14,10 @@ namespace mrg8g {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 // Shared-memory words per warp for lane_window of layout V (the eight
-// states, then the window values of the lane's V substreams).
+// states, then the window values of the lane's V substreams), and for
+// lane_window_rows (the values only).
 MRG8G_HDC constexpr int window_scratch(int V) { return 64 + 8 * V * 32; }
+MRG8G_HDC constexpr int window_rows_scratch(int V) { return 8 * V * 32; }
 
 // Output kinds; the numbering is part of the C ABI (include/mrg8g.h).
 enum Kind : int { kU32 = 0, kF64Orig = 1, kF64Shift = 2, kF32Orig = 3, kF32Shift = 4 };
@@ -219,6 +221,42 @@ __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, co
 #pragma unroll
         for (int j = 0; j < 8; ++j) x[v][j] = xs[(v * 8 + j) * 32 + lane];
     __syncwarp();  // the scratch words are free again
+}
+
+// The same window from 8 V rows of the window table per lane (row
+// e_0^T A^(o + 1 + d j) against s itself), four rows at a time, through the
+// warp's scratch ([slot][lane], 8 V * 32 words).  Four table round trips
+// instead of one, but fewer instructions and a lower register peak: the
+// batch kernel uses it for launches with more tiles than warps, where the
+// setup's latency hides behind other warps' work and the main loop's speed
+// counts (10,000 uneven instances: 886 against 876 Goutputs/s).  `scratch`
+// holds window_rows_scratch(V) words.
+template <int V, int ELEM, bool LAG_MOD>
+__device__ __forceinline__ void lane_window_rows(const uint32_t* __restrict__ win, const uint32_t s[8], int lane,
+                                                 uint32_t* scratch, uint32_t (&x)[V][8]) {
+    const uint32_t* w = win + win_offset(layout_index(V));
+#pragma unroll 1
+    for (int i0 = 0; i0 < 8 * V; i0 += 4) {
+        uint4 r[8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + q, v = i >> 3, j = i & 7;
+            const uint4* row = reinterpret_cast<const uint4*>(w + (sub_offset<V, ELEM>(lane, v) * 8 + j) * 8);
+            r[2 * q] = __ldg(row);
+            r[2 * q + 1] = __ldg(row + 1);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 r0 = r[2 * q], r1 = r[2 * q + 1];
+            const uint32_t rv[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
+            const uint32_t S = dot8_ref(rv, s);  // [1, p], or 0 for residue 0
+            scratch[(i0 + q) * 32 + lane] = LAG_MOD ? lag_mod(S) : lag_minus1(S);
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[v][j] = scratch[(v * 8 + j) * 32 + lane];  // the lane's own words
 }
 
 }  // namespace mrg8g

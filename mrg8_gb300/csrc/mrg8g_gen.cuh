@@ -74,8 +74,10 @@ __device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const 
 
 // The run of `len` outputs from state s (see the file comment).  `out` must
 // be 16-byte aligned when V > 1; `scratch` is the warp's window_scratch(V)
-// words of shared memory (16-byte aligned).
-template <int V, int KIND>
+// words of shared memory (16-byte aligned).  QUICK_SETUP picks the window
+// setup of one table round trip (lane_window) over the row-table form
+// (lane_window_rows).
+template <int V, int KIND, bool QUICK_SETUP = true>
 __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, const uint32_t* __restrict__ dstep,
                                               const uint32_t s[8], typename OutOf<KIND>::T* out, uint64_t len,
                                               const LeapCoef& lc, uint32_t* scratch) {
@@ -84,7 +86,8 @@ __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, 
     constexpr bool kAluTail = sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
-    lane_window<V, sizeof(T), kLagMod<KIND>>(win, dstep, s, lane, scratch, x);
+    if constexpr (QUICK_SETUP) lane_window<V, sizeof(T), kLagMod<KIND>>(win, dstep, s, lane, scratch, x);
+    else lane_window_rows<V, sizeof(T), kLagMod<KIND>>(win, s, lane, scratch, x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
     T* const p = out + sub_offset<V, sizeof(T)>((uint32_t)lane, 0);
