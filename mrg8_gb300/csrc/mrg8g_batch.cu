@@ -24,13 +24,20 @@ namespace mrg8g {
 
 MRG8G_DEFINE_TABLE_UPLOAD(upload_tables_batch)
 
+// Tiles shorter than this many outputs (256 rows) form their windows in one
+// table round trip even in a launch with more tiles than warps: there the
+// setup is a large part of the tile (65,536 tiles of 4,096 outputs: 818
+// against 754 Goutputs/s), while long tiles run about 1 % faster with the
+// row-table setup.
+constexpr uint32_t kQuickSetupElems = 256u * 32u * kBatchLayoutV;
+
 template <int KIND, bool QUICK>
 __device__ __forceinline__ void run_tile(const BatchInst& in, const BatchTile& t, const uint32_t s[8],
                                          const BatchArgs& a, uint32_t* scratch) {
     using T = typename OutOf<KIND>::T;
     T* out = static_cast<T*>(in.out) + t.start;
-    warp_generate<kBatchLayoutV, KIND, QUICK>(g_win, g_dstep, s, out, t.len_flags, a.leap[kLagMod<KIND> ? 1 : 0],
-                                              scratch);
+    warp_generate<kBatchLayoutV, KIND>(g_win, g_dstep, s, out, t.len_flags, a.leap[kLagMod<KIND> ? 1 : 0], scratch,
+                                       QUICK || t.len_flags < kQuickSetupElems);
 }
 
 template <int KIND>
@@ -84,14 +91,14 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // QUICK: a launch with no more tiles than warps (launch_batch decides), whose
 // time is its latency: each warp takes the tile of its own index in the grid
 // (no wait on the counter) and forms its window in one table round trip.
-// Otherwise warps pull tiles from the counter and use the row-table window,
-// the faster form when the setup's latency hides behind other warps' work
-// (10,000 uneven instances: 896 Goutputs/s against 876 with the QUICK forms).
+// Otherwise warps pull tiles from the counter, and long tiles use the
+// row-table window, the faster form when the setup's latency hides behind
+// other warps' work (10,000 uneven instances: 888 Goutputs/s against 876
+// with the QUICK forms).
 template <int THREADS, bool QUICK>
 __global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const __grid_constant__ BatchArgs a) {
     if (a.times && blockIdx.x == 0 && threadIdx.x == 0) a.times[0] = global_ns();
-    __shared__ __align__(16) uint32_t
-        scratch[THREADS / 32][QUICK ? window_scratch(kBatchLayoutV) : window_rows_scratch(kBatchLayoutV)];
+    __shared__ __align__(16) uint32_t scratch[THREADS / 32][window_scratch(kBatchLayoutV)];
     const int lane = threadIdx.x & 31;
     uint32_t* sc = scratch[threadIdx.x >> 5];
     for (int round = 0;; ++round) {

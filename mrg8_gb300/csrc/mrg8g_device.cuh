@@ -14,10 +14,9 @@ namespace mrg8g {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 // Shared-memory words per warp for lane_window of layout V (the eight
-// states, then the window values of the lane's V substreams), and for
-// lane_window_rows (the values only).
+// states, then the window values of the lane's V substreams; lane_window_rows
+// uses the values' part only).
 MRG8G_HDC constexpr int window_scratch(int V) { return 64 + 8 * V * 32; }
-MRG8G_HDC constexpr int window_rows_scratch(int V) { return 8 * V * 32; }
 
 // Output kinds; the numbering is part of the C ABI (include/mrg8g.h).
 enum Kind : int { kU32 = 0, kF64Orig = 1, kF64Shift = 2, kF32Orig = 3, kF32Shift = 4 };
@@ -229,8 +228,8 @@ __device__ __forceinline__ void lane_window(const uint32_t* __restrict__ win, co
 // instead of one, but fewer instructions and a lower register peak: the
 // batch kernel uses it for launches with more tiles than warps, where the
 // setup's latency hides behind other warps' work and the main loop's speed
-// counts (10,000 uneven instances: 886 against 876 Goutputs/s).  `scratch`
-// holds window_rows_scratch(V) words.
+// counts (10,000 uneven instances: 888 against 876 Goutputs/s).  `scratch`
+// holds at least 8 V * 32 words.
 template <int V, int ELEM, bool LAG_MOD>
 __device__ __forceinline__ void lane_window_rows(const uint32_t* __restrict__ win, const uint32_t s[8], int lane,
                                                  uint32_t* scratch, uint32_t (&x)[V][8]) {

@@ -74,19 +74,19 @@ __device__ __forceinline__ void store_checked(typename OutOf<KIND>::T* p, const 
 
 // The run of `len` outputs from state s (see the file comment).  `out` must
 // be 16-byte aligned when V > 1; `scratch` is the warp's window_scratch(V)
-// words of shared memory (16-byte aligned).  QUICK_SETUP picks the window
-// setup of one table round trip (lane_window) over the row-table form
-// (lane_window_rows).
-template <int V, int KIND, bool QUICK_SETUP = true>
+// words of shared memory (16-byte aligned).  quick_setup (lane-uniform) picks
+// the window setup of one table round trip (lane_window) over the row-table
+// form (lane_window_rows).
+template <int V, int KIND>
 __device__ __forceinline__ void warp_generate(const uint32_t* __restrict__ win, const uint32_t* __restrict__ dstep,
                                               const uint32_t s[8], typename OutOf<KIND>::T* out, uint64_t len,
-                                              const LeapCoef& lc, uint32_t* scratch) {
+                                              const LeapCoef& lc, uint32_t* scratch, bool quick_setup = true) {
     using T = typename OutOf<KIND>::T;
     constexpr uint32_t D = 32 * V;
     constexpr bool kAluTail = sizeof(T) == 4;
     const int lane = threadIdx.x & 31;
     uint32_t x[V][8];
-    if constexpr (QUICK_SETUP) lane_window<V, sizeof(T), kLagMod<KIND>>(win, dstep, s, lane, scratch, x);
+    if (quick_setup) lane_window<V, sizeof(T), kLagMod<KIND>>(win, dstep, s, lane, scratch, x);
     else lane_window_rows<V, sizeof(T), kLagMod<KIND>>(win, s, lane, scratch, x);
 
     const uint64_t rows = (len + D - 1) / D, full = len / D;
