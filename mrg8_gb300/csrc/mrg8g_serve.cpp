@@ -8,11 +8,15 @@
 // admitted as soon as a stream slot and arena space are free and their work
 // overlaps on the device.  Generator states live in a device table; a draw
 // from a registered generator continues its stream (the host keeps only the
-// position).  Each launch records an event; while launches are in flight the
-// scheduler polls their events (and yields between polls), which takes a
-// completion within about a microsecond of the batch's end, and it blocks on
-// a condition variable only when nothing is in flight.  Nothing on the device
-// waits: the kernels are the batch kernel and every host wait is bounded.
+// position).  A launch is complete when its kernel's end stamp reaches mapped
+// host memory (the last block writes it after every block fenced its
+// outputs); its completion event is queried too, every sixteenth check and
+// for launches without a kernel, so that errors surface.  While launches are
+// in flight the scheduler polls (and yields between polls); it blocks on a
+// condition variable only when nothing is in flight.  The arena places blocks
+// first-fit (mrg8g_arena.h), so space released in any order is reused.
+// Nothing on the device waits: the kernels are the batch kernel and every
+// host wait is bounded.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -197,8 +201,8 @@ int enqueue_slot(mrg8g_server* sv, Slot& sl, const std::vector<BatchInst>& insts
 }
 
 // Kernel interval of a finished launch against the recent ones (lock held;
-// the launch's completion event has been seen, so the kernel's stamps are
-// in host memory).  A launch that overlaps an earlier one counts both, once
+// the launch's end stamp or completion event has been seen, so the kernel's
+// stamps are in host memory).  A launch that overlaps an earlier one counts both, once
 // each.  Launches without a kernel (no tiles) have no stamps.
 void note_interval(mrg8g_server* sv, Slot& sl) {
     const unsigned long long a = sl.h_times[0], b = sl.h_times[1];
@@ -559,9 +563,11 @@ int mrg8g_server_read(mrg8g_server* sv, uint64_t ticket, void* host, uint64_t by
         src = static_cast<const char*>(sv->arena_base) + q.arena_off;
     }
     // A plain blocking copy: the request is done, i.e. the scheduler has seen
-    // the completion event of its launch, so its outputs are complete in
-    // device memory and no ordering with the launch's (non-blocking) stream is
-    // needed.  The region stays the request's until mrg8g_server_release.
+    // its launch complete (the kernel's end stamp, written after every block
+    // fenced its outputs, or the launch's completion event), so its outputs are
+    // complete in device memory and no ordering with the launch's
+    // (non-blocking) stream is needed.  The region stays the request's until
+    // mrg8g_server_release.
     cudaError_t e = cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "serving: result read");
     return MRG8G_SUCCESS;
