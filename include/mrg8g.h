@@ -227,6 +227,10 @@ MRG8G_API int mrg8g_batch_generate_noalloc(const mrg8g_instance *inst, uint64_t 
 MRG8G_API int mrg8g_batch_autotune(mrg8g_batch *b, void *stream, mrg8g_batch_config *chosen);
 
 MRG8G_API int mrg8g_batch_get_config(const mrg8g_batch *b, mrg8g_batch_config *cfg);
+/* Change the launch shape.  A new tiling rewrites the plan's device
+ * descriptors, so this first waits for the plan's last launch (on whatever
+ * stream it went); a launch made while its stream was capturing is not
+ * tracked: do not change the plan while a graph that holds it may run. */
 MRG8G_API int mrg8g_batch_set_config(mrg8g_batch *b, const mrg8g_batch_config *cfg);
 MRG8G_API int mrg8g_batch_stats(const mrg8g_batch *b, uint64_t *tiles, uint64_t *outputs, uint64_t *bytes);
 MRG8G_API int mrg8g_batch_destroy(mrg8g_batch *b);

@@ -93,6 +93,10 @@ struct mrg8g_batch {
     uint64_t ntiles = 0;
     cudaStream_t cap = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // Recorded after every launch outside a stream capture: a re-plan waits
+    // for it before it rewrites the descriptors or drops the graph, which a
+    // launch on the caller's (possibly non-blocking) stream may still read.
+    cudaEvent_t last = nullptr;
 };
 
 namespace {
@@ -173,6 +177,10 @@ int apply_config(mrg8g_batch* b, const mrg8g_batch_config& c) {
     mrg8g_batch_config n = c;
     int rc = normalise(n);
     if (rc) return rc;
+    if (b->last) {
+        const cudaError_t e = cudaEventSynchronize(b->last);
+        if (e != cudaSuccess) return cuda_fail(e, "waiting for the plan's last launch");
+    }
     const bool retile = n.tile_rows != b->cfg.tile_rows || n.tiling != b->cfg.tiling || !b->planned;
     if (retile) {
         const uint64_t total =
@@ -257,6 +265,7 @@ int build_graph(mrg8g_batch* b) {
 }
 
 void destroy_plan(mrg8g_batch* b) {
+    if (b->last) cudaEventSynchronize(b->last), cudaEventDestroy(b->last);
     release_graph(b);
     if (b->cap) cudaStreamDestroy(b->cap);
     if (b->d_insts) cudaFree(b->d_insts);
@@ -411,11 +420,21 @@ int mrg8g_batch_launch(mrg8g_batch* b, void* stream) {
     if (!b->planned) return fail(MRG8G_ERR_INVALID_STATE, "the batch has no valid plan (a re-plan failed)");
     if (!b->ntiles) return MRG8G_SUCCESS;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!b->cfg.use_graph) return enqueue(b, s);
     int rc;
-    if (!b->exec && (rc = build_graph(b))) return rc;
-    cudaError_t e = cudaGraphLaunch(b->exec, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    if (!b->cfg.use_graph) {
+        if ((rc = enqueue(b, s))) return rc;
+    } else {
+        if (!b->exec && (rc = build_graph(b))) return rc;
+        cudaError_t e = cudaGraphLaunch(b->exec, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(s, &cs);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone) return MRG8G_SUCCESS;  // captured: no real record to wait for
+    if (!b->last && (e = cudaEventCreateWithFlags(&b->last, cudaEventDisableTiming)) != cudaSuccess)
+        return cuda_fail(e, "cudaEventCreate");
+    if ((e = cudaEventRecord(b->last, s)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     return MRG8G_SUCCESS;
 }
 
