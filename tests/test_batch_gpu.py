@@ -75,6 +75,34 @@ def test_batch_matches_oracle(cuda, oracle):
     assert st["outputs"] == sum(x[2] for x in meta)
 
 
+def test_replan_right_after_a_launch_on_a_non_blocking_stream(cuda, oracle):
+    """Outputs cleared and a launch enqueued on a side stream, then at once a
+    re-plan (new tile rows and tiling) from the host: the re-plan waits for
+    the launch before it rewrites the descriptors, so the launch still writes
+    every output of the old plan; repeated over four plans."""
+    import torch
+
+    import mrg8_gb300 as m
+    rng = np.random.default_rng(31)
+    insts, meta = make_instances(cuda, rng, 60, 20)
+    want = [expected(oracle, st, off, n, kind).view(np.uint8) for st, off, n, kind, _, _ in meta]
+    b = m.Batch(insts, tile_rows=64)
+    side = torch.cuda.Stream()
+    plans = ((64, 0), (16, 1), (512, 0), (32, 1), (64, 0))
+    for k in range(len(plans) - 1):
+        torch.cuda.synchronize()
+        with torch.cuda.stream(side):
+            for _, _, n, _, buf, lead in meta:
+                buf[lead:lead + n].zero_()
+        b.launch(stream=side)
+        b.set_config(tile_rows=plans[k + 1][0], tiling=plans[k + 1][1])
+        torch.cuda.synchronize()
+        for (st, off, n, kind, buf, lead), w in zip(meta, want):
+            assert np.array_equal(as_bytes(buf[lead:lead + n]), w), (k, n, kind, off)
+    check_canaries(meta)
+    b.close()
+
+
 def test_batch_relaunch_autotune_and_plain_launch_agree(cuda, oracle):
     import torch
     import mrg8_gb300 as m
