@@ -60,7 +60,7 @@ public:
         free_[at] = size;
     }
     uint64_t used() const { return used_; }
-    // Largest free range (for tests and diagnostics).
+    // Largest free range (merged ranges: equals the largest gap between live blocks).
     uint64_t largest_free() const {
         uint64_t m = 0;
         for (const auto& f : free_) m = f.second > m ? f.second : m;

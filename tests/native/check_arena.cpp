@@ -74,6 +74,7 @@ int main() {
                 live.erase(live.begin() + (long)k);
             }
             if (a.used() != used) return fail("used", a.used(), used);
+            if (a.largest_free() != largest_gap(live, cap)) return fail("largest free range", a.largest_free(), largest_gap(live, cap));
         }
         std::shuffle(live.begin(), live.end(), rng);
         for (const Live& l : live) a.release(l.seq);
