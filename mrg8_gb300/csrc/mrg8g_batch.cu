@@ -63,24 +63,6 @@ __device__ __forceinline__ uint32_t tile_owner(const uint32_t* __restrict__ base
     return lo;
 }
 
-// Tile ti of a device-tiled launch (see BatchArgs).
-__device__ __forceinline__ BatchTile derive_tile(const BatchArgs& a, uint32_t ti, const BatchInst& in, uint32_t i) {
-    const uint32_t elem = (in.kind == kF64Orig || in.kind == kF64Shift) ? 8u : 4u;
-    uint64_t head = ((16u - (uint32_t)((uintptr_t)in.out & 15u)) & 15u) / elem;
-    if (head > in.n) head = in.n;
-    const uint32_t li = ti - a.tile_base[i];
-    BatchTile t;
-    t.inst = i;
-    if (head && li == 0) {
-        t.start = 0;
-        t.len_flags = (uint32_t)head | kTileHead;
-    } else {
-        t.start = head + (uint64_t)(li - (head ? 1u : 0u)) * a.tile_elems;
-        const uint64_t left = in.n - t.start;
-        t.len_flags = (uint32_t)(left < a.tile_elems ? left : a.tile_elems);
-    }
-    return t;
-}
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -120,7 +102,7 @@ __global__ void __launch_bounds__(THREADS, THREADS == 128 ? 9 : 4) k_batch(const
         } else {
             const uint32_t i = tile_owner(a.tile_base, a.ninst, ti);
             in = a.insts[i];
-            t = derive_tile(a, ti, in, i);
+            t = derive_tile(ti - a.tile_base[i], in, i, a.tile_elems);
         }
         const uint32_t* src = in.slot1 ? a.states + 8ull * (in.slot1 - 1) : in.st;
         uint32_t s[8];
@@ -240,22 +222,17 @@ int noalloc_scratch(int dev, void** out) {
     return MRG8G_SUCCESS;
 }
 
-// Tiles written straight into the staging area (no heap): heads first, then
-// body tiles; the largest-first order of make_tiles by an in-place sort.
+// Tiles written straight into the staging area (no heap), cut as every plan
+// cuts them (mrg8g_tiles.h); the largest-first order of make_tiles by an
+// in-place sort.
 int noalloc_tiles(const BatchInst* insts, uint32_t count, BatchTile* tiles, uint32_t* ntiles) {
     uint32_t k = 0;
+    const uint64_t T = (uint64_t)kNoAllocTileRows * 32 * (uint64_t)kBatchLayoutV;
     for (uint32_t i = 0; i < count; ++i) {
-        const BatchInst& in = insts[i];
-        if (in.n == 0) continue;
-        const int elem = kind_elem_bytes(in.kind);
-        const uint64_t T = (uint64_t)kNoAllocTileRows * 32 * (uint64_t)kBatchLayoutV;
-        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
-        if (head > in.n) head = in.n;
-        const uint64_t body = (in.n - head + T - 1) / T;
-        if ((uint64_t)k + (head ? 1 : 0) + body > MRG8G_NOALLOC_MAX_TILES)
+        const uint64_t m = instance_tiles(insts[i], T);
+        if ((uint64_t)k + m > MRG8G_NOALLOC_MAX_TILES)
             return fail(MRG8G_ERR_BUDGET, "batch needs more than %d tiles (the no-alloc limit)", MRG8G_NOALLOC_MAX_TILES);
-        if (head) tiles[k++] = {0, i, (uint32_t)head | kTileHead};
-        for (uint64_t s = head; s < in.n; s += T) tiles[k++] = {s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)};
+        for (uint64_t li = 0; li < m; ++li) tiles[k++] = derive_tile((uint32_t)li, insts[i], i, (uint32_t)T);
     }
     std::sort(tiles, tiles + k, [&](const BatchTile& x, const BatchTile& y) {
         const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(insts[x.inst].kind);

@@ -16,65 +16,6 @@
 
 using namespace mrg8g;
 
-namespace mrg8g {
-
-// Tiles of every instance: an unaligned head (fewer outputs than one 16-byte
-// vector) and body tiles of tile_rows rows; ordered by bytes, largest first,
-// so the dynamic queue ends with the smallest pieces.
-void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vector<BatchTile>& tiles) {
-    tiles.clear();
-    for (uint32_t i = 0; i < count; ++i) {
-        const BatchInst& in = insts[i];
-        if (in.n == 0) continue;
-        const int elem = kind_elem_bytes(in.kind);
-        const uint64_t T = (uint64_t)tile_rows * 32 * kBatchLayoutV;
-        uint64_t head = ((16 - (uintptr_t)in.out % 16) % 16) / elem;
-        if (head > in.n) head = in.n;
-        if (head) tiles.push_back({0, i, (uint32_t)head | kTileHead});
-        for (uint64_t s = head; s < in.n; s += T) tiles.push_back({s, i, (uint32_t)std::min<uint64_t>(T, in.n - s)});
-    }
-    std::stable_sort(tiles.begin(), tiles.end(), [&](const BatchTile& x, const BatchTile& y) {
-        const uint64_t bx = (uint64_t)(x.len_flags & ~kTileHead) * kind_elem_bytes(insts[x.inst].kind);
-        const uint64_t by = (uint64_t)(y.len_flags & ~kTileHead) * kind_elem_bytes(insts[y.inst].kind);
-        return bx > by;
-    });
-}
-
-void sort_largest_first(BatchInst* insts, uint32_t count) {
-    std::stable_sort(insts, insts + count, [](const BatchInst& x, const BatchInst& y) {
-        return x.n * kind_elem_bytes(x.kind) > y.n * kind_elem_bytes(y.kind);
-    });
-}
-
-// Tiles of a plan with body tiles of tile_elems outputs (both tilings cut the
-// instances the same way), counted without building them.
-uint64_t count_tiles(const BatchInst* insts, uint32_t count, uint64_t tile_elems) {
-    uint64_t total = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-        const BatchInst& d = insts[i];
-        if (!d.n) continue;
-        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
-        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
-        total += (head ? 1 : 0) + (d.n - head + tile_elems - 1) / tile_elems;
-    }
-    return total;
-}
-
-uint64_t tile_prefix(const BatchInst* insts, uint32_t count, uint64_t tile_elems, uint32_t* base) {
-    uint64_t total = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-        base[i] = (uint32_t)total;
-        const BatchInst& d = insts[i];
-        if (!d.n) continue;
-        const uint64_t elem = (uint64_t)kind_elem_bytes(d.kind);
-        const uint64_t head = std::min<uint64_t>(((16 - (uintptr_t)d.out % 16) % 16) / elem, d.n);
-        total += (head ? 1 : 0) + (d.n - head + tile_elems - 1) / tile_elems;
-    }
-    base[count] = (uint32_t)total;
-    return total;
-}
-
-}  // namespace mrg8g
 
 struct mrg8g_batch {
     int dev = -1;
@@ -153,7 +94,7 @@ int plan_derived(mrg8g_batch* b) {
 }
 
 void build_tiles(mrg8g_batch* b) {
-    make_tiles(b->insts.data(), (uint32_t)b->insts.size(), b->cfg.tile_rows, b->tiles);
+    make_tiles(b->insts.data(), (uint32_t)b->insts.size(), (uint64_t)b->cfg.tile_rows * 32 * kBatchLayoutV, b->tiles);
 }
 
 int upload_tiles(mrg8g_batch* b) {

@@ -50,13 +50,7 @@ int launch_plain_call(const uint32_t st[8], void* d_out, uint64_t n, int kind, c
 
 cudaError_t upload_tables_batch();
 
-// Tiles of a batch (see mrg8g_batch_host.cpp).
-void make_tiles(const BatchInst* insts, uint32_t count, int tile_rows, std::vector<BatchTile>& tiles);
-// Device-derived tiling: instances ordered longest (in bytes) first, and the
-// prefix counts of their tiles with body tiles of tile_elems outputs
-// (base[i] = first tile of instance i, base[count] = the total, which the
-// return value gives in 64 bits so that callers can reject overflow).
-void sort_largest_first(BatchInst* insts, uint32_t count);
-uint64_t tile_prefix(const BatchInst* insts, uint32_t count, uint64_t tile_elems, uint32_t* base);
-
 }  // namespace mrg8g
+
+// Tiles of a batch: make_tiles, sort_largest_first, count_tiles, tile_prefix.
+#include "mrg8g_tiles.h"
